@@ -1,0 +1,345 @@
+#!/usr/bin/env python
+"""LC2 similarity benchmark: evals/s at 256^3 on one GB300.
+
+Workload (one "step"): one batched launch of K = 512 candidate affine
+transforms of a 256^3 MR volume into a 256^3 US volume, 9^3 patches
+(PatchSize 4), FP16 storage of both volumes, FP32 arithmetic with exact
+64-bit fixed-point patch moments. The volumes are synthetic and seeded
+(ellipsoid MR phantom, US synthesised from it with Rayleigh speckle, 10% of
+the US replaced by constant 16^3 blocks).
+
+Reported:
+  value      batched evals/s, device-timed (CUDA events on the library's
+             stream), inputs resident in HBM, L2 flushed between steps;
+  e2e        the same through the public C ABI call lc2_evaluate_batch with
+             host transforms in and host results out (H2D/D2H inside);
+  plain      one evaluation per lc2_evaluate call (the reference's
+             one-eval-per-objective form) on the same GPU;
+  roofline   the moments kernel (the dominant one): algorithmic bytes
+             (K*N*s_mov + N*s_fix per launch group) / its event-timed
+             duration, against the measured HBM copy bandwidth;
+  cpu_baseline  the FP64 oracle (a port of the reference formulas; the
+             reference has no CPU LC2 path) on the host cores.
+
+`--impl reference` times that CPU port alone on the same workload.
+Multi-GPU: independent replicas (one process per GPU, no collective on the
+data path); value = total evals / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "LC2 evals/s at 256^3 (batched, 512 affines/launch, 9^3 patches, FP16 storage)"
+UNIT = "evals/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--candidates", type=int, default=512)
+    ap.add_argument("--patch", type=int, default=4)
+    ap.add_argument("--storage", default="f16", choices=["f32", "f16", "bf16"])
+    ap.add_argument("--plain-evals", type=int, default=16)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def workload(args):
+    from lc2registration_gb300 import synth
+
+    case = synth.case_3d(seed=2024, mr_size=args.size, us_size=args.size, r=args.patch,
+                         constant_block_frac=0.1)
+    import numpy as np
+
+    from tests.helpers import perturbed
+
+    mats = perturbed(case, np.random.default_rng(77), args.candidates, scale=1.0)
+    return case, mats
+
+
+def config_dict(args, case):
+    return {
+        "workload": f"3D affine, MR {args.size}^3 -> US {args.size}^3 at 1 mm, PatchSize "
+                    f"{args.patch} ({2 * args.patch + 1}^3 patches), {args.candidates} candidate "
+                    f"affines per launch, {args.storage} storage, 10% constant US blocks",
+        "virtual_voxels": int(case.fixed_geom.n),
+        "candidates_per_step": args.candidates,
+        "patch_size": args.patch,
+        "storage": args.storage,
+        "l2": "flushed between steps (256 MiB write); per-step working set > L2",
+        "parallelism": "replicas" if args.gpus > 1 else "single GPU",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", self.gpu_id, f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                mx.append(float(p[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_port(case, mats, seconds: float, storage: str):
+    """FP64 oracle on the host cores over a bounded sample of candidates."""
+    from tests.helpers import oracle_eval
+
+    t0 = time.perf_counter()
+    done = 0
+    while True:
+        oracle_eval(case, mats[done % len(mats)], storage=storage)
+        done += 1
+        el = time.perf_counter() - t0
+        if el >= seconds and done >= 2:
+            break
+    return done / el, done, el
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+
+    O.build()
+    case, mats = workload(args)
+    cores = os.cpu_count() or 1
+    from tests.helpers import oracle_eval
+
+    for w in range(args.warmup):
+        oracle_eval(case, mats[w % len(mats)], storage=args.storage)
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        oracle_eval(case, mats[s % len(mats)], storage=args.storage)
+    total = time.perf_counter() - t0
+    value = args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": config_dict(args, case),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full {args.size}^3 evaluations (one per step) "
+                                   "of the FP64 oracle, OpenMP over all host cores; the reference "
+                                   "has no CPU LC2 implementation"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    from lc2registration_gb300 import capi
+
+    capi.load()
+    case, mats = workload(args)
+    ctx = capi.Context(case.mode, case.fixed_geom, case.moving_geom, case.virt_spacing, case.r,
+                       case.hr_moving, args.storage, device=local)
+    ctx.set_images(case.fixed, case.moving)
+    K = mats.shape[0]
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")
+
+    ctx.stage(mats)
+    for _ in range(args.warmup):
+        ctx.launch(K)
+    torch.cuda.synchronize()
+
+    props = torch.cuda.get_device_properties(local)
+    gpu_id = str(getattr(props, "uuid", local))
+    if gpu_id and not gpu_id.startswith("GPU-") and len(gpu_id) > 8:
+        gpu_id = "GPU-" + gpu_id
+    # ---- timed region: K steps, device events per step, L2 flushed between ----
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    launches0 = ctx.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(gpu_id) as clk:
+        with torch.cuda.stream(stream):
+            for s in range(args.steps):
+                flush.zero_()
+                ev[s][0].record(stream)
+                ctx.launch(K)
+                ev[s][1].record(stream)
+        torch.cuda.synchronize()
+    launches = ctx.launch_count() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * K * args.steps / (total_ms / 1e3)
+    res = ctx.fetch(K)
+    assert np.all(np.isfinite(res)) and res.max() > 0
+
+    # ---- per-kernel timing of one step (roofline) ----
+    ctx.enable_kernel_timing(True)
+    ctx.launch(K)
+    kt = ctx.kernel_times()
+    ctx.enable_kernel_timing(False)
+    n_vox = case.fixed_geom.n
+    s_mov = 4 if args.storage == "f32" else 2
+    s_fix = s_mov
+    mom_ms, mom_launches = kt["moments"]
+    alg_bytes = K * n_vox * s_mov + mom_launches * n_vox * s_fix
+    achieved = alg_bytes / (mom_ms / 1e3) / 1e9
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "moments_traffic.json")
+    if os.path.exists(tfile):
+        try:
+            traffic = json.load(open(tfile)).get("bytes_per_launch_scaled")
+        except Exception:
+            traffic = None
+
+    # ---- e2e through the public call, host buffers ----
+    e2e_t = 0.0
+    for s in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = ctx.evaluate_batch(mats)
+        e2e_t += time.perf_counter() - t0
+    e2e = world * K * args.steps / e2e_t if world == 1 else None
+    if dist:
+        t = torch.tensor([e2e_t], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e = world * K * args.steps / float(t.item())
+    assert np.array_equal(out, res), "batched results changed between runs"
+
+    # ---- plain form: one evaluation per call ----
+    P = min(args.plain_evals, K)
+    for m in mats[:2]:
+        ctx.evaluate(m)
+    t0 = time.perf_counter()
+    plain_vals = [ctx.evaluate(m) for m in mats[:P]]
+    plain_t = time.perf_counter() - t0
+    plain_eps = P / plain_t
+    assert np.array_equal(np.array(plain_vals), res[:P]), "plain != batched"
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as O
+
+        O.build()
+        eps, n, el = cpu_port(case, mats, args.cpu_seconds, args.storage)
+        cpu = {"value": eps, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{n} full {args.size}^3 evaluations of the FP64 oracle over "
+                         f"{el:.1f} s (OpenMP, all host cores); the reference has no CPU LC2 path"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic",
+            "config": config_dict(args, case),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_moments", "kernel_ms_per_launch": mom_ms / max(1, mom_launches),
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
+            "kernels_ms_per_step": {k: v[0] for k, v in kt.items()},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": K * 96,
+                    "d2h_bytes_per_step": K * 8},
+            "plain": {"value": plain_eps, "unit": UNIT, "evals": P,
+                      "batched_over_plain": value / world / plain_eps},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "lc2_true_transform": float(ctx.evaluate(case.true_mat)),
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

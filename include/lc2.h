@@ -1,0 +1,154 @@
+/*
+ * lc2.h -- C ABI of the GB300 LC2 similarity library (liblc2.so).
+ *
+ * Drop-in boundary for the similarity hot path of LC2Registration. The
+ * reference exposes C++ classes, not a C ABI; each entry point below names
+ * the reference interface it replaces (paths relative to the reference
+ * project root). All entry points return an lc2_status (0 = success); the
+ * message of the last failure on the calling thread is lc2_last_error().
+ *
+ * Conventions:
+ *   - images/volumes are float32, x fastest (index x + y*X + z*X*Y), the
+ *     reference's layout; 2D images use dim[2] = 1;
+ *   - transforms are row-major virtual->moving mm matrices: 3x3 (9 floats)
+ *     in 2D mode, 4x4 (16 floats) in 3D and 2D-to-3D modes -- the matrix
+ *     the reference uploads as VirtualToMoving{2,3}D_d
+ *     (src/Interpolator/interpolator.cuh:32-41);
+ *   - a context owns its device memory and one CUDA stream; there is no
+ *     process-global state, so contexts are independent and thread-safe
+ *     per context (the reference keeps geometry in process-global
+ *     __constant__ symbols, src/Interpolator/interpolator.cuh:27-41).
+ */
+#ifndef LC2_H
+#define LC2_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    LC2_OK = 0,
+    LC2_ERR_INVALID_ARGUMENT = 1, /* bad dims, patch size, null pointer, NaN/Inf input */
+    LC2_ERR_OUT_OF_MEMORY = 2,    /* device or host allocation failed */
+    LC2_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+    LC2_ERR_NOT_READY = 4,        /* images not set yet */
+    LC2_ERR_SINGULAR = 5,         /* non-invertible transform */
+    LC2_ERR_UNSUPPORTED = 6       /* mode/patch size outside the supported range */
+} lc2_status;
+
+typedef enum { LC2_MODE_2D = 0, LC2_MODE_3D = 1, LC2_MODE_2DTO3D = 2 } lc2_mode;
+
+/* Storage type of the gathered (moving) volume and of the static ultrasound
+ * image on the device; arithmetic is FP32/integer regardless. */
+typedef enum { LC2_STORE_F32 = 0, LC2_STORE_F16 = 1, LC2_STORE_BF16 = 2 } lc2_storage;
+
+typedef struct {
+    int dim[3];        /* voxels; 2D images: dim[2] = 1 */
+    float spacing[3];  /* mm */
+    float origin[3];   /* mm */
+} lc2_geometry;
+
+typedef struct {
+    int mode;                /* lc2_mode */
+    lc2_geometry fixed;      /* FixedImage / FixedVolume */
+    lc2_geometry moving;     /* MovingImage / MovingVolume */
+    float virtual_spacing[3];/* RegistrationParameters.ResampledSpacing */
+    int patch_size;          /* RegistrationParameters.PatchSize (radius r, patch 2r+1) */
+    int high_res_is_moving;  /* HighResolutionModality: 1 = Moving, 0 = Fixed */
+    int storage;             /* lc2_storage */
+    int max_batch;           /* transforms per launch group; 0 = automatic */
+    int device;              /* CUDA device ordinal */
+} lc2_config;
+
+typedef struct lc2_context lc2_context;
+
+/* Creates a context: virtual grid, device buffers, stream.
+ * Replaces Interpolator{2D,3D,2DTo3D}::Interpolator{...}(const LC2Configuration*)
+ * + InitiateMappers + InitiateRegistrationHandle
+ * (src/Interpolator/interpolator.cu:393-529, :1105-1246, :1538-1676) and
+ * LC2_{2D,3D}_class::PortedFromInterpolator (src/cu_LC2/cu_lc2_2d.cu:515-546,
+ * src/cu_LC2/cu_lc2_3d.cu:942-975). */
+int lc2_create(const lc2_config* cfg, lc2_context** out);
+
+/* Releases all device memory and the stream of the context. */
+int lc2_destroy(lc2_context* ctx);
+
+/* Uploads fixed and moving images (host float32) and precomputes the
+ * static virtual-grid image. Replaces the FixedVolume_d / MovingVolume_d
+ * uploads (src/Interpolator/interpolator.cu:276,315,459-473). */
+int lc2_set_images(lc2_context* ctx, const float* fixed_host, const float* moving_host);
+
+/* Virtual grid dims (src/Interpolator/interpolator.cu:337-339). */
+int lc2_virtual_dims(const lc2_context* ctx, int dims[3]);
+
+/* One LC2 evaluation for one transform (the plain form). Replaces the
+ * per-objective sequence GenerateMappers -> Interpolate ->
+ * GetSimilarityMeasure (src/Optimizers/optimizers.cu:170-176,702-707;
+ * src/Interpolator/interpolator.cu:542-631; src/cu_LC2/cu_lc2_3d.cu:1119-1194).
+ * *lc2_out = sum(measure)/sum(sigma), 0 when NaN/Inf. */
+int lc2_evaluate(lc2_context* ctx, const float* matrix, double* lc2_out);
+
+/* `count` evaluations (matrices packed back to back). Batched form of
+ * lc2_evaluate; results are identical to `count` plain calls. */
+int lc2_evaluate_batch(lc2_context* ctx, const float* matrices, int count, double* lc2_out);
+
+/* Asynchronous pieces of lc2_evaluate_batch, for callers that time or
+ * overlap the device work: stage copies the matrices to the device, launch
+ * enqueues every kernel on the context stream, fetch copies results back and
+ * synchronises the stream. */
+int lc2_stage_transforms(lc2_context* ctx, const float* matrices, int count);
+int lc2_launch_staged(lc2_context* ctx, int count);
+int lc2_fetch_results(lc2_context* ctx, double* lc2_out, int count);
+
+/* The context's CUDA stream (a cudaStream_t), and an override with a
+ * caller-owned stream (NULL restores the context's own stream). */
+void* lc2_get_stream(const lc2_context* ctx);
+int lc2_set_stream(lc2_context* ctx, void* stream);
+
+/* Diagnostic evaluation that also downloads the per-voxel virtual-grid
+ * fields (any pointer may be NULL): ultrasound U, high-resolution image M,
+ * its Sobel magnitude G, weighting factor sigma and clipped measure.
+ * Mirrors the buffers behind LC2_{2D,3D}_class::Get*Buffer/Get*RawPointer
+ * (src/cu_LC2/cu_lc2_2d.cu:821-831, src/cu_LC2/cu_lc2_3d.cu:1331-1345). */
+int lc2_evaluate_fields(lc2_context* ctx, const float* matrix, double* lc2_out, float* U,
+                        float* M, float* G, float* sigma, float* measure);
+
+/* Kernel launches issued by this context since creation (device work
+ * accounting for benchmarks). */
+long long lc2_launch_count(const lc2_context* ctx);
+
+/* Per-kernel device timing with CUDA events on the context stream (off by
+ * default). lc2_kernel_times synchronises, returns the summed milliseconds
+ * and launch counts of the resampling, Sobel and moments kernels since the
+ * last call (index 0, 1, 2), and resets them. */
+int lc2_enable_kernel_timing(lc2_context* ctx, int on);
+int lc2_kernel_times(lc2_context* ctx, double ms[3], long long counts[3]);
+
+/* Transform builders. Replace Spatial3DMapper::AffineInit / RigidInit
+ * (src/Interpolator/spatialMappers.cuh:585-850) and Spatial2DMapper::AffineInit
+ * (:999-1033): x_m = L (x_v - C + shift) + C + T, L = Rz Ry Rx Sh S (3D),
+ * L = R Sh S (2D). Angles in degrees; outputs row-major float matrices. */
+int lc2_affine_3d(const float rotation[3], const float translation[3], const float scale[3],
+                  const float shear[3], const float center[3], const float shift[3],
+                  float out[16]);
+int lc2_affine_2d(float rotation, const float translation[2], const float scale[2], float shear,
+                  const float center[2], const float shift[2], float out[9]);
+
+/* Inverse of a row-major affine 4x4 (bottom row 0 0 0 1). Replaces
+ * InvertS4X4Matrix (src/Utilities/my_cuda_helper.cu:395-523) and
+ * Spatial3DMapper::GetMyselfInversed (spatialMappers.cuh:315-433). Returns
+ * LC2_ERR_SINGULAR when the determinant is 0. */
+int lc2_invert_affine_3d(const float in[16], float out[16]);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char* lc2_last_error(void);
+
+/* Library version string. */
+const char* lc2_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

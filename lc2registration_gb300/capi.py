@@ -1,0 +1,262 @@
+"""ctypes binding of liblc2.so (the C ABI in include/lc2.h).
+
+Loading fails loudly when the library has not been built: there is no CPU
+fallback for the LC2 path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import build as _build
+from .geometry import Geometry
+
+LC2_OK = 0
+STATUS_NAMES = {
+    0: "LC2_OK",
+    1: "LC2_ERR_INVALID_ARGUMENT",
+    2: "LC2_ERR_OUT_OF_MEMORY",
+    3: "LC2_ERR_CUDA",
+    4: "LC2_ERR_NOT_READY",
+    5: "LC2_ERR_SINGULAR",
+    6: "LC2_ERR_UNSUPPORTED",
+}
+MODES = {"2D": 0, "3D": 1, "2DTo3D": 2}
+STORAGE = {"f32": 0, "f16": 1, "bf16": 2}
+
+# Every symbol include/lc2.h declares (checked by the test suite).
+EXPORTED = [
+    "lc2_create", "lc2_destroy", "lc2_set_images", "lc2_virtual_dims", "lc2_evaluate",
+    "lc2_evaluate_batch", "lc2_stage_transforms", "lc2_launch_staged", "lc2_fetch_results",
+    "lc2_get_stream", "lc2_set_stream", "lc2_evaluate_fields", "lc2_launch_count",
+    "lc2_enable_kernel_timing", "lc2_kernel_times",
+    "lc2_affine_3d", "lc2_affine_2d", "lc2_invert_affine_3d", "lc2_last_error", "lc2_version",
+]
+
+
+class LC2Error(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class lc2_geometry(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int * 3), ("spacing", ctypes.c_float * 3),
+                ("origin", ctypes.c_float * 3)]
+
+
+class lc2_config(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int), ("fixed", lc2_geometry), ("moving", lc2_geometry),
+                ("virtual_spacing", ctypes.c_float * 3), ("patch_size", ctypes.c_int),
+                ("high_res_is_moving", ctypes.c_int), ("storage", ctypes.c_int),
+                ("max_batch", ctypes.c_int), ("device", ctypes.c_int)]
+
+
+_fp = ctypes.POINTER(ctypes.c_float)
+_dp = ctypes.POINTER(ctypes.c_double)
+_lib = None
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load liblc2.so (building it with nvcc if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB_PATH
+    if build_if_missing and _build.needs_build():
+        _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError(f"liblc2.so is not built ({path}); run lc2registration_gb300.build")
+    lib = ctypes.CDLL(path)
+    vp = ctypes.c_void_p
+    sig = {
+        "lc2_create": ([ctypes.POINTER(lc2_config), ctypes.POINTER(vp)], ctypes.c_int),
+        "lc2_destroy": ([vp], ctypes.c_int),
+        "lc2_set_images": ([vp, _fp, _fp], ctypes.c_int),
+        "lc2_virtual_dims": ([vp, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "lc2_evaluate": ([vp, _fp, _dp], ctypes.c_int),
+        "lc2_evaluate_batch": ([vp, _fp, ctypes.c_int, _dp], ctypes.c_int),
+        "lc2_stage_transforms": ([vp, _fp, ctypes.c_int], ctypes.c_int),
+        "lc2_launch_staged": ([vp, ctypes.c_int], ctypes.c_int),
+        "lc2_fetch_results": ([vp, _dp, ctypes.c_int], ctypes.c_int),
+        "lc2_get_stream": ([vp], vp),
+        "lc2_set_stream": ([vp, vp], ctypes.c_int),
+        "lc2_evaluate_fields": ([vp, _fp, _dp, _fp, _fp, _fp, _fp, _fp], ctypes.c_int),
+        "lc2_launch_count": ([vp], ctypes.c_longlong),
+        "lc2_enable_kernel_timing": ([vp, ctypes.c_int], ctypes.c_int),
+        "lc2_kernel_times": ([vp, _dp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+        "lc2_affine_3d": ([_fp, _fp, _fp, _fp, _fp, _fp, _fp], ctypes.c_int),
+        "lc2_affine_2d": ([ctypes.c_float, _fp, _fp, ctypes.c_float, _fp, _fp, _fp], ctypes.c_int),
+        "lc2_invert_affine_3d": ([_fp, _fp], ctypes.c_int),
+        "lc2_last_error": ([], ctypes.c_char_p),
+        "lc2_version": ([], ctypes.c_char_p),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def _check(status: int):
+    if status != LC2_OK:
+        raise LC2Error(status, load().lc2_last_error().decode())
+
+
+def _geom(g: Geometry) -> lc2_geometry:
+    out = lc2_geometry()
+    for a in range(3):
+        out.dim[a] = int(g.dim[a])
+        out.spacing[a] = float(g.spacing[a])
+        out.origin[a] = float(g.origin[a])
+    return out
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Context:
+    """One LC2 evaluation context (fixed + moving image on one GPU)."""
+
+    def __init__(self, mode: str, fixed_geom: Geometry, moving_geom: Geometry,
+                 virt_spacing: Sequence[float], patch_size: int, high_res_is_moving: bool = True,
+                 storage: str = "f32", max_batch: int = 0, device: int = 0):
+        lib = load()
+        cfg = lc2_config()
+        cfg.mode = MODES[mode]
+        cfg.fixed = _geom(fixed_geom)
+        cfg.moving = _geom(moving_geom)
+        vs = list(virt_spacing) + [1.0] * (3 - len(virt_spacing))
+        for a in range(3):
+            cfg.virtual_spacing[a] = float(vs[a])
+        cfg.patch_size = int(patch_size)
+        cfg.high_res_is_moving = int(bool(high_res_is_moving))
+        cfg.storage = STORAGE[storage]
+        cfg.max_batch = int(max_batch)
+        cfg.device = int(device)
+        self.mode = mode
+        self.matrix_size = 9 if mode == "2D" else 16
+        self._h = ctypes.c_void_p()
+        _check(lib.lc2_create(ctypes.byref(cfg), ctypes.byref(self._h)))
+        self._lib = lib
+
+    def close(self):
+        if self._h:
+            self._lib.lc2_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_images(self, fixed: np.ndarray, moving: np.ndarray):
+        f, m = _f32(fixed), _f32(moving)
+        _check(self._lib.lc2_set_images(self._h, f.ctypes.data_as(_fp), m.ctypes.data_as(_fp)))
+
+    def virtual_dims(self):
+        d = (ctypes.c_int * 3)()
+        _check(self._lib.lc2_virtual_dims(self._h, d))
+        return tuple(d)
+
+    def _mats(self, mats) -> np.ndarray:
+        m = _f32(mats).reshape(-1, self.matrix_size)
+        return m
+
+    def evaluate(self, mat) -> float:
+        m = self._mats(mat)
+        out = ctypes.c_double()
+        _check(self._lib.lc2_evaluate(self._h, m.ctypes.data_as(_fp), ctypes.byref(out)))
+        return out.value
+
+    def evaluate_batch(self, mats) -> np.ndarray:
+        m = self._mats(mats)
+        out = np.empty(m.shape[0], dtype=np.float64)
+        _check(self._lib.lc2_evaluate_batch(self._h, m.ctypes.data_as(_fp), m.shape[0],
+                                            out.ctypes.data_as(_dp)))
+        return out
+
+    def stage(self, mats) -> int:
+        m = self._mats(mats)
+        _check(self._lib.lc2_stage_transforms(self._h, m.ctypes.data_as(_fp), m.shape[0]))
+        return m.shape[0]
+
+    def launch(self, count: int):
+        _check(self._lib.lc2_launch_staged(self._h, int(count)))
+
+    def fetch(self, count: int) -> np.ndarray:
+        out = np.empty(count, dtype=np.float64)
+        _check(self._lib.lc2_fetch_results(self._h, out.ctypes.data_as(_dp), int(count)))
+        return out
+
+    def stream(self) -> int:
+        return self._lib.lc2_get_stream(self._h) or 0
+
+    def set_stream(self, stream_ptr: Optional[int]):
+        _check(self._lib.lc2_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
+
+    def launch_count(self) -> int:
+        return int(self._lib.lc2_launch_count(self._h))
+
+    def enable_kernel_timing(self, on: bool = True):
+        _check(self._lib.lc2_enable_kernel_timing(self._h, int(bool(on))))
+
+    def kernel_times(self):
+        """{'warp'|'sobel'|'moments': (total ms, launches)} since the last call."""
+        ms = (ctypes.c_double * 3)()
+        cnt = (ctypes.c_longlong * 3)()
+        _check(self._lib.lc2_kernel_times(self._h, ms, cnt))
+        return {k: (ms[i], int(cnt[i])) for i, k in enumerate(("warp", "sobel", "moments"))}
+
+    def evaluate_fields(self, mat):
+        """Returns (lc2, dict of per-voxel float32 fields U, M, G, sigma, measure)."""
+        m = self._mats(mat)
+        d = self.virtual_dims()
+        n = d[0] * d[1] * d[2]
+        f = {k: np.empty(n, dtype=np.float32) for k in ("U", "M", "G", "sigma", "measure")}
+        out = ctypes.c_double()
+        _check(self._lib.lc2_evaluate_fields(
+            self._h, m.ctypes.data_as(_fp), ctypes.byref(out),
+            *[f[k].ctypes.data_as(_fp) for k in ("U", "M", "G", "sigma", "measure")]))
+        return out.value, f
+
+
+def affine_3d(rot, trans, scale=(1, 1, 1), shear=(0, 0, 0), center=(0, 0, 0), shift=(0, 0, 0)):
+    lib = load()
+    args = [_f32(v) for v in (rot, trans, scale, shear, center, shift)]
+    out = np.zeros(16, dtype=np.float32)
+    _check(lib.lc2_affine_3d(*[a.ctypes.data_as(_fp) for a in args], out.ctypes.data_as(_fp)))
+    return out.reshape(4, 4)
+
+
+def affine_2d(rot, trans, scale=(1, 1), shear=0.0, center=(0, 0), shift=(0, 0)):
+    lib = load()
+    t, s, c, sh = (_f32(v) for v in (trans, scale, center, shift))
+    out = np.zeros(9, dtype=np.float32)
+    _check(lib.lc2_affine_2d(float(rot), t.ctypes.data_as(_fp), s.ctypes.data_as(_fp), float(shear),
+                             c.ctypes.data_as(_fp), sh.ctypes.data_as(_fp), out.ctypes.data_as(_fp)))
+    return out.reshape(3, 3)
+
+
+def invert_affine_3d(mat) -> np.ndarray:
+    lib = load()
+    m = _f32(mat).ravel()
+    out = np.zeros(16, dtype=np.float32)
+    _check(lib.lc2_invert_affine_3d(m.ctypes.data_as(_fp), out.ctypes.data_as(_fp)))
+    return out.reshape(4, 4)

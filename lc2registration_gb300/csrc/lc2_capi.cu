@@ -1,0 +1,807 @@
+// lc2_capi.cu -- context management, launch sequencing and the C ABI
+// declared in include/lc2.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "../../include/lc2.h"
+#include "lc2_kernels.cuh"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define LC2_CUDA(call)                                                                     \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) {                                                               \
+      if (e_ == cudaErrorMemoryAllocation)                                                 \
+        return fail(LC2_ERR_OUT_OF_MEMORY, "%s: %s", #call, cudaGetErrorString(e_));       \
+      return fail(LC2_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                  __LINE__);                                                               \
+    }                                                                                      \
+  } while (0)
+
+#define LC2_TRY(expr)         \
+  do {                        \
+    int s_ = (expr);          \
+    if (s_ != LC2_OK) return s_; \
+  } while (0)
+
+size_t elem_size(int storage) { return storage == LC2_STORE_F32 ? 4 : 2; }
+
+}  // namespace
+
+struct lc2_context {
+  lc2_config cfg{};
+  int warp_nd = 3;  // dimensionality of the resampling
+  int lc2_nd = 3;   // dimensionality of Sobel / patches
+  lc2_geometry virt{};
+  size_t nv = 0, nf = 0, nm = 0;  // voxels: virtual, fixed, moving
+  int n = 0;                      // patch voxels
+  int qbits = 0;
+  bool ready = false;
+
+  // device buffers
+  void* d_moving = nullptr;    // storage type, nm
+  void* d_static = nullptr;    // hr_moving: U in storage type; hr_fixed: M as float
+  float* d_gstatic = nullptr;  // hr_fixed: Sobel(M)
+  float* d_scratch = nullptr;  // per-slot warped image (+ Sobel when hr_moving)
+  int slots = 1;
+  lc2::Xform* d_xf = nullptr;
+  unsigned long long* d_acc = nullptr;
+  double* d_out = nullptr;
+  int cap = 0;  // capacity of d_xf/d_acc/d_out (transforms)
+  lc2::Xform* h_xf = nullptr;  // pinned staging
+  double* h_out = nullptr;     // pinned results
+  int staged = 0;
+
+  lc2::MomentParams mp{};
+  float vmax_u = 0, vmax_m = 0, vmax_g = 0;
+
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  long long launches = 0;
+
+  // optional per-kernel timing (lc2_enable_kernel_timing)
+  bool timing = false;
+  struct Timed {
+    int kind;
+    cudaEvent_t a, b;
+  };
+  std::vector<Timed> timed;
+};
+
+namespace {
+
+// Kernel kinds for lc2_kernel_times.
+enum { K_WARP = 0, K_SOBEL = 1, K_MOMENTS = 2, K_KINDS = 3 };
+
+struct TimerScope {
+  lc2_context* c;
+  int kind;
+  cudaEvent_t a = nullptr, b = nullptr;
+  TimerScope(lc2_context* c_, int kind_) : c(c_), kind(kind_) {
+    if (!c->timing) return;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+      a = b = nullptr;
+      return;
+    }
+    cudaEventRecord(a, c->stream);
+  }
+  ~TimerScope() {
+    if (!a) return;
+    cudaEventRecord(b, c->stream);
+    c->timed.push_back({kind, a, b});
+  }
+};
+
+int select_device(const lc2_context* c) {
+  int cur = -1;
+  LC2_CUDA(cudaGetDevice(&cur));
+  if (cur != c->cfg.device) LC2_CUDA(cudaSetDevice(c->cfg.device));
+  return LC2_OK;
+}
+
+bool finite_geom(const lc2_geometry& g) {
+  for (int a = 0; a < 3; ++a) {
+    if (g.dim[a] < 1) return false;
+    if (!std::isfinite(g.spacing[a]) || !(g.spacing[a] > 0.0f)) return false;
+    if (!std::isfinite(g.origin[a])) return false;
+  }
+  return true;
+}
+
+// Moving-pixel affine of virtual voxels (see lc2::Xform).
+void build_xform(int nd, const lc2_geometry& v, const lc2_geometry& m, const float* mat,
+                 lc2::Xform* X) {
+  double L[3][3] = {{0}}, t[3] = {0};
+  if (nd == 2) {
+    for (int a = 0; a < 2; ++a) {
+      L[a][0] = mat[3 * a + 0];
+      L[a][1] = mat[3 * a + 1];
+      t[a] = mat[3 * a + 2];
+    }
+  } else {
+    for (int a = 0; a < 3; ++a) {
+      for (int b = 0; b < 3; ++b) L[a][b] = mat[4 * a + b];
+      t[a] = mat[4 * a + 3];
+    }
+  }
+  for (int a = 0; a < 3; ++a) {
+    double bsum = t[a] - (double)m.origin[a];
+    for (int b = 0; b < 3; ++b) {
+      X->A[3 * a + b] = L[a][b] * (double)v.spacing[b] / (double)m.spacing[a];
+      bsum += L[a][b] * (double)v.origin[b];
+    }
+    X->b[a] = bsum / (double)m.spacing[a];
+    if (nd == 2 && a == 2) {
+      X->A[6] = X->A[7] = X->A[8] = 0.0;
+      X->b[2] = 0.0;
+    }
+  }
+  if (nd == 2) {
+    X->A[2] = 0.0;
+    X->A[5] = 0.0;
+  }
+}
+
+long long floor_clamp(long double v) {
+  if (v >= (long double)std::numeric_limits<long long>::max()) return std::numeric_limits<long long>::max();
+  if (v < 0) return -1;
+  return (long long)std::floor(v);
+}
+
+int ensure_capacity(lc2_context* c, int count) {
+  if (count <= c->cap) return LC2_OK;
+  int ncap = std::max(count, std::max(64, c->cap * 2));
+  if (c->d_xf) cudaFree(c->d_xf);
+  if (c->d_acc) cudaFree(c->d_acc);
+  if (c->d_out) cudaFree(c->d_out);
+  if (c->h_xf) cudaFreeHost(c->h_xf);
+  if (c->h_out) cudaFreeHost(c->h_out);
+  c->d_xf = nullptr; c->d_acc = nullptr; c->d_out = nullptr; c->h_xf = nullptr; c->h_out = nullptr;
+  c->cap = 0;
+  LC2_CUDA(cudaMalloc(&c->d_xf, sizeof(lc2::Xform) * ncap));
+  LC2_CUDA(cudaMalloc(&c->d_acc, sizeof(unsigned long long) * 2 * ncap));
+  LC2_CUDA(cudaMalloc(&c->d_out, sizeof(double) * ncap));
+  LC2_CUDA(cudaMallocHost(&c->h_xf, sizeof(lc2::Xform) * ncap));
+  LC2_CUDA(cudaMallocHost(&c->h_out, sizeof(double) * ncap));
+  c->cap = ncap;
+  return LC2_OK;
+}
+
+template <typename T>
+int launch_convert(lc2_context* c, const float* in, void* out, size_t n) {
+  int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+  lc2::k_convert<T><<<blocks, 256, 0, c->stream>>>(in, reinterpret_cast<T*>(out), n);
+  ++c->launches;
+  LC2_CUDA(cudaGetLastError());
+  return LC2_OK;
+}
+
+int convert_to_storage(lc2_context* c, const float* in, void* out, size_t n, int storage) {
+  if (storage == LC2_STORE_F16) return launch_convert<__half>(c, in, out, n);
+  if (storage == LC2_STORE_BF16) return launch_convert<__nv_bfloat16>(c, in, out, n);
+  return launch_convert<float>(c, in, out, n);
+}
+
+template <typename T>
+__global__ void k_tofloat(const T* __restrict__ in, float* __restrict__ out, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t step = (size_t)gridDim.x * blockDim.x;
+  for (; i < n; i += step) out[i] = lc2::ldf(in, i);
+}
+
+int to_float(lc2_context* c, const void* in, float* out, size_t n, int storage) {
+  int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+  if (storage == LC2_STORE_F16)
+    k_tofloat<__half><<<blocks, 256, 0, c->stream>>>((const __half*)in, out, n);
+  else if (storage == LC2_STORE_BF16)
+    k_tofloat<__nv_bfloat16><<<blocks, 256, 0, c->stream>>>((const __nv_bfloat16*)in, out, n);
+  else
+    k_tofloat<float><<<blocks, 256, 0, c->stream>>>((const float*)in, out, n);
+  ++c->launches;
+  LC2_CUDA(cudaGetLastError());
+  return LC2_OK;
+}
+
+template <typename TM>
+int launch_warp_t(lc2_context* c, int nd, const TM* src, const lc2_geometry& sg, const lc2::Xform* xf,
+                  int k0, int cnt, float* out, size_t slot_stride) {
+  const lc2_geometry& v = c->virt;
+  dim3 block(32, 8, 1);
+  dim3 grid((v.dim[0] + 31) / 32, (v.dim[1] + 7) / 8, v.dim[2] * cnt);
+  TimerScope ts(c, K_WARP);
+  if (nd == 3)
+    lc2::k_warp<3, TM><<<grid, block, 0, c->stream>>>(src, sg.dim[0], sg.dim[1], sg.dim[2],
+                                                      v.dim[0], v.dim[1], v.dim[2], xf, k0, out,
+                                                      slot_stride);
+  else
+    lc2::k_warp<2, TM><<<grid, block, 0, c->stream>>>(src, sg.dim[0], sg.dim[1], sg.dim[2],
+                                                      v.dim[0], v.dim[1], v.dim[2], xf, k0, out,
+                                                      slot_stride);
+  ++c->launches;
+  LC2_CUDA(cudaGetLastError());
+  return LC2_OK;
+}
+
+int launch_warp(lc2_context* c, int nd, const void* src, int storage, const lc2_geometry& sg,
+                const lc2::Xform* xf, int k0, int cnt, float* out, size_t slot_stride) {
+  if (storage == LC2_STORE_F16)
+    return launch_warp_t<__half>(c, nd, (const __half*)src, sg, xf, k0, cnt, out, slot_stride);
+  if (storage == LC2_STORE_BF16)
+    return launch_warp_t<__nv_bfloat16>(c, nd, (const __nv_bfloat16*)src, sg, xf, k0, cnt, out,
+                                        slot_stride);
+  return launch_warp_t<float>(c, nd, (const float*)src, sg, xf, k0, cnt, out, slot_stride);
+}
+
+int launch_sobel(lc2_context* c, const float* in, float* out, int cnt, size_t slot_stride) {
+  const lc2_geometry& v = c->virt;
+  dim3 block(32, 8, 1);
+  dim3 grid((v.dim[0] + 31) / 32, (v.dim[1] + 7) / 8, v.dim[2] * cnt);
+  TimerScope ts(c, K_SOBEL);
+  if (c->lc2_nd == 3)
+    lc2::k_sobel<3><<<grid, block, 0, c->stream>>>(in, v.dim[0], v.dim[1], v.dim[2], out,
+                                                   slot_stride);
+  else
+    lc2::k_sobel<2><<<grid, block, 0, c->stream>>>(in, v.dim[0], v.dim[1], v.dim[2], out,
+                                                   slot_stride);
+  ++c->launches;
+  LC2_CUDA(cudaGetLastError());
+  return LC2_OK;
+}
+
+template <int ND, typename TU>
+int launch_moments_t(lc2_context* c, const TU* U, const float* M, const float* G,
+                     const lc2::MomentParams& P, int k0, int cnt, float* osig, float* omeas) {
+  const lc2_geometry& v = c->virt;
+  size_t smem = lc2::mom_smem_bytes(P.r);
+  LC2_CUDA(cudaFuncSetAttribute(lc2::k_moments<ND, TU>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((v.dim[0] + lc2::kTX - 1) / lc2::kTX, (v.dim[1] + lc2::kTY - 1) / lc2::kTY,
+            P.nzchunks * cnt);
+  TimerScope ts(c, K_MOMENTS);
+  lc2::k_moments<ND, TU><<<grid, lc2::kNT, smem, c->stream>>>(U, M, G, P, c->d_acc, k0, osig,
+                                                              omeas);
+  ++c->launches;
+  LC2_CUDA(cudaGetLastError());
+  return LC2_OK;
+}
+
+template <int ND>
+int launch_moments_nd(lc2_context* c, const void* U, int ustore, const float* M, const float* G,
+                      const lc2::MomentParams& P, int k0, int cnt, float* osig, float* omeas) {
+  if (ustore == LC2_STORE_F16)
+    return launch_moments_t<ND, __half>(c, (const __half*)U, M, G, P, k0, cnt, osig, omeas);
+  if (ustore == LC2_STORE_BF16)
+    return launch_moments_t<ND, __nv_bfloat16>(c, (const __nv_bfloat16*)U, M, G, P, k0, cnt, osig,
+                                               omeas);
+  return launch_moments_t<ND, float>(c, (const float*)U, M, G, P, k0, cnt, osig, omeas);
+}
+
+// z-chunking: enough CTAs to fill the GPU with a small priming overhead
+void choose_zchunks(const lc2_context* c, int cnt, lc2::MomentParams& P) {
+  if (c->lc2_nd == 2) {
+    P.zchunk = 1;
+    P.nzchunks = 1;
+    return;
+  }
+  const lc2_geometry& v = c->virt;
+  long long tiles = (long long)((v.dim[0] + lc2::kTX - 1) / lc2::kTX) *
+                    ((v.dim[1] + lc2::kTY - 1) / lc2::kTY) * cnt;
+  long long want = 152LL * 6;
+  int nz = (int)std::max<long long>(1, (want + tiles - 1) / tiles);
+  int min_chunk = std::max(8, 2 * P.r + 1);
+  nz = std::min(nz, std::max(1, v.dim[2] / min_chunk));
+  nz = std::min(nz, 65535 / std::max(1, cnt));
+  P.zchunk = (v.dim[2] + nz - 1) / nz;
+  P.nzchunks = (v.dim[2] + P.zchunk - 1) / P.zchunk;
+}
+
+// Enqueue the evaluation of staged transforms [k0, k0 + cnt), cnt <= slots.
+int launch_group(lc2_context* c, int k0, int cnt, float* osig, float* omeas) {
+  const size_t nv = c->nv;
+  lc2::MomentParams P = c->mp;
+  choose_zchunks(c, cnt, P);
+  float* w = c->d_scratch;  // warped image, slot stride nv
+  if (c->cfg.high_res_is_moving) {
+    float* g = c->d_scratch + (size_t)c->slots * nv;  // Sobel of it
+    LC2_TRY(launch_warp(c, c->warp_nd, c->d_moving, c->cfg.storage, c->cfg.moving, c->d_xf, k0, cnt,
+                        w, nv));
+    LC2_TRY(launch_sobel(c, w, g, cnt, nv));
+    P.u_stride = 0;
+    P.m_stride = nv;
+    P.g_stride = nv;
+    if (c->lc2_nd == 3)
+      return launch_moments_nd<3>(c, c->d_static, c->cfg.storage, w, g, P, k0, cnt, osig, omeas);
+    return launch_moments_nd<2>(c, c->d_static, c->cfg.storage, w, g, P, k0, cnt, osig, omeas);
+  }
+  LC2_TRY(launch_warp(c, c->warp_nd, c->d_moving, c->cfg.storage, c->cfg.moving, c->d_xf, k0, cnt,
+                      w, nv));
+  P.u_stride = nv;
+  P.m_stride = 0;
+  P.g_stride = 0;
+  if (c->lc2_nd == 3)
+    return launch_moments_nd<3>(c, w, LC2_STORE_F32, (const float*)c->d_static, c->d_gstatic, P,
+                                k0, cnt, osig, omeas);
+  return launch_moments_nd<2>(c, w, LC2_STORE_F32, (const float*)c->d_static, c->d_gstatic, P, k0,
+                              cnt, osig, omeas);
+}
+
+int matrix_floats(const lc2_context* c) { return c->warp_nd == 2 ? 9 : 16; }
+
+int check_ctx(const lc2_context* c) {
+  if (!c) return fail(LC2_ERR_INVALID_ARGUMENT, "null context");
+  if (!c->ready) return fail(LC2_ERR_NOT_READY, "images not set (call lc2_set_images first)");
+  return LC2_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lc2_last_error(void) { return g_err.c_str(); }
+
+const char* lc2_version(void) { return "lc2-gb300 0.1 (sm_103a)"; }
+
+int lc2_create(const lc2_config* cfg, lc2_context** out) {
+  g_err.clear();
+  if (!cfg || !out) return fail(LC2_ERR_INVALID_ARGUMENT, "null config or output pointer");
+  *out = nullptr;
+  if (cfg->mode < LC2_MODE_2D || cfg->mode > LC2_MODE_2DTO3D)
+    return fail(LC2_ERR_INVALID_ARGUMENT, "unknown mode %d", cfg->mode);
+  if (cfg->storage < LC2_STORE_F32 || cfg->storage > LC2_STORE_BF16)
+    return fail(LC2_ERR_INVALID_ARGUMENT, "unknown storage %d", cfg->storage);
+  if (!finite_geom(cfg->fixed) || !finite_geom(cfg->moving))
+    return fail(LC2_ERR_INVALID_ARGUMENT, "geometry needs dims >= 1, finite spacing > 0 and origin");
+  for (int a = 0; a < 3; ++a)
+    if (!std::isfinite(cfg->virtual_spacing[a]) || !(cfg->virtual_spacing[a] > 0.0f))
+      if (!(cfg->mode == LC2_MODE_2D && a == 2))
+        return fail(LC2_ERR_INVALID_ARGUMENT, "virtual spacing must be finite and > 0");
+  lc2_context* c = new (std::nothrow) lc2_context();
+  if (!c) return fail(LC2_ERR_OUT_OF_MEMORY, "host allocation failed");
+  c->cfg = *cfg;
+  c->warp_nd = (cfg->mode == LC2_MODE_2D) ? 2 : 3;
+  c->lc2_nd = (cfg->mode == LC2_MODE_3D) ? 3 : 2;
+  if (cfg->mode == LC2_MODE_2D) {
+    c->cfg.fixed.dim[2] = 1;
+    c->cfg.moving.dim[2] = 1;
+  }
+  // virtual grid: fixed origin, dims ceil(dimF * spF / spV) in float
+  // (src/Interpolator/interpolator.cu:337-339, :1093-1094, :1603-1605)
+  for (int a = 0; a < 3; ++a) {
+    c->virt.origin[a] = c->cfg.fixed.origin[a];
+    c->virt.spacing[a] = cfg->virtual_spacing[a];
+    if (a < c->warp_nd) {
+      float ext = (float)c->cfg.fixed.dim[a] * c->cfg.fixed.spacing[a];
+      c->virt.dim[a] = (int)std::ceil((double)(ext / cfg->virtual_spacing[a]));
+    } else {
+      c->virt.dim[a] = 1;
+      c->virt.spacing[a] = 1.0f;
+      c->virt.origin[a] = 0.0f;
+    }
+  }
+  int r = cfg->patch_size;
+  int rmax = (c->lc2_nd == 3) ? 6 : 12;
+  if (r < 1 || r > rmax) {
+    delete c;
+    return fail(LC2_ERR_UNSUPPORTED, "patch size %d outside [1, %d] for %dD patches", r, rmax,
+                c->lc2_nd);
+  }
+  if (cfg->mode == LC2_MODE_2DTO3D && c->virt.dim[2] != 1) {
+    delete c;
+    return fail(LC2_ERR_INVALID_ARGUMENT,
+                "2D-to-3D needs a single virtual slice (fixed z extent <= virtual z spacing)");
+  }
+  c->nv = (size_t)c->virt.dim[0] * c->virt.dim[1] * c->virt.dim[2];
+  c->nf = (size_t)c->cfg.fixed.dim[0] * c->cfg.fixed.dim[1] * c->cfg.fixed.dim[2];
+  c->nm = (size_t)c->cfg.moving.dim[0] * c->cfg.moving.dim[1] * c->cfg.moving.dim[2];
+  c->n = (2 * r + 1) * (2 * r + 1) * (c->lc2_nd == 3 ? (2 * r + 1) : 1);
+  // fixed-point bits: n * 2^(b+1) <= 2^31 (int32 first-order sums with one
+  // bit of headroom; then n^2 2^(2b) <= 2^60 for the centred int64 sums)
+  int b = 0;
+  while (b < 21 && ((long long)c->n << (b + 2)) <= (1LL << 31)) ++b;
+  c->qbits = b;
+
+  int st = select_device(c);
+  if (st != LC2_OK) {
+    delete c;
+    return st;
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(LC2_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+  }
+  c->stream = c->own_stream;
+  // scratch slots: warped image (+ its Sobel when the moving image is the
+  // high-resolution one), within a 1 GiB budget unless max_batch says more
+  size_t per_slot = c->nv * sizeof(float) * (cfg->high_res_is_moving ? 2 : 1);
+  long long slots = cfg->max_batch > 0 ? cfg->max_batch
+                                       : std::max<long long>(1, (1LL << 30) / (long long)per_slot);
+  slots = std::min<long long>(slots, 1024);
+  slots = std::min<long long>(slots, 65535 / c->virt.dim[2]);
+  c->slots = (int)std::max<long long>(1, slots);
+  e = cudaMalloc(&c->d_scratch, per_slot * c->slots);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_moving, c->nm * elem_size(cfg->storage));
+  if (e == cudaSuccess)
+    e = cudaMalloc(&c->d_static,
+                   c->nv * (cfg->high_res_is_moving ? elem_size(cfg->storage) : sizeof(float)));
+  if (e == cudaSuccess && !cfg->high_res_is_moving)
+    e = cudaMalloc(&c->d_gstatic, c->nv * sizeof(float));
+  if (e != cudaSuccess) {
+    lc2_destroy(c);
+    return fail(LC2_ERR_OUT_OF_MEMORY, "device allocation: %s", cudaGetErrorString(e));
+  }
+  st = ensure_capacity(c, 64);
+  if (st != LC2_OK) {
+    std::string msg = g_err;
+    lc2_destroy(c);
+    g_err = msg;
+    return st;
+  }
+  *out = c;
+  return LC2_OK;
+}
+
+int lc2_destroy(lc2_context* c) {
+  if (!c) return LC2_OK;
+  select_device(c);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  cudaFree(c->d_moving);
+  cudaFree(c->d_static);
+  cudaFree(c->d_gstatic);
+  cudaFree(c->d_scratch);
+  cudaFree(c->d_xf);
+  cudaFree(c->d_acc);
+  cudaFree(c->d_out);
+  if (c->h_xf) cudaFreeHost(c->h_xf);
+  if (c->h_out) cudaFreeHost(c->h_out);
+  for (auto& t : c->timed) {
+    cudaEventDestroy(t.a);
+    cudaEventDestroy(t.b);
+  }
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+  return LC2_OK;
+}
+
+int lc2_virtual_dims(const lc2_context* c, int dims[3]) {
+  if (!c || !dims) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  for (int a = 0; a < 3; ++a) dims[a] = c->virt.dim[a];
+  return LC2_OK;
+}
+
+void* lc2_get_stream(const lc2_context* c) { return c ? (void*)c->stream : nullptr; }
+
+int lc2_set_stream(lc2_context* c, void* stream) {
+  if (!c) return fail(LC2_ERR_INVALID_ARGUMENT, "null context");
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return LC2_OK;
+}
+
+long long lc2_launch_count(const lc2_context* c) { return c ? c->launches : 0; }
+
+int lc2_enable_kernel_timing(lc2_context* c, int on) {
+  if (!c) return fail(LC2_ERR_INVALID_ARGUMENT, "null context");
+  c->timing = on != 0;
+  return LC2_OK;
+}
+
+int lc2_kernel_times(lc2_context* c, double ms[3], long long counts[3]) {
+  if (!c || !ms || !counts) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  LC2_TRY(select_device(c));
+  LC2_CUDA(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < K_KINDS; ++k) {
+    ms[k] = 0.0;
+    counts[k] = 0;
+  }
+  for (auto& t : c->timed) {
+    float e = 0.0f;
+    if (cudaEventElapsedTime(&e, t.a, t.b) == cudaSuccess) {
+      ms[t.kind] += e;
+      counts[t.kind] += 1;
+    }
+    cudaEventDestroy(t.a);
+    cudaEventDestroy(t.b);
+  }
+  c->timed.clear();
+  return LC2_OK;
+}
+
+int lc2_set_images(lc2_context* c, const float* fixed, const float* moving) {
+  g_err.clear();
+  if (!c || !fixed || !moving) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  LC2_TRY(select_device(c));
+  float fmax = 0.0f, mmax = 0.0f;
+  for (size_t i = 0; i < c->nf; ++i) {
+    if (!std::isfinite(fixed[i])) return fail(LC2_ERR_INVALID_ARGUMENT, "fixed image has NaN/Inf at %zu", i);
+    fmax = std::max(fmax, std::fabs(fixed[i]));
+  }
+  for (size_t i = 0; i < c->nm; ++i) {
+    if (!std::isfinite(moving[i])) return fail(LC2_ERR_INVALID_ARGUMENT, "moving image has NaN/Inf at %zu", i);
+    mmax = std::max(mmax, std::fabs(moving[i]));
+  }
+  const int storage = c->cfg.storage;
+  // stage both images as float on the device, then convert
+  float* tmp = nullptr;
+  size_t tmp_n = std::max(c->nf, c->nm);
+  LC2_CUDA(cudaMalloc(&tmp, sizeof(float) * tmp_n));
+  struct Free {
+    float* p;
+    ~Free() { cudaFree(p); }
+  } guard{tmp};
+  // moving volume in storage type
+  LC2_CUDA(cudaMemcpyAsync(tmp, moving, sizeof(float) * c->nm, cudaMemcpyHostToDevice, c->stream));
+  LC2_TRY(convert_to_storage(c, tmp, c->d_moving, c->nm, storage));
+  // fixed volume resampled onto the virtual grid through the identity
+  // (VirtualToFixed, src/Interpolator/interpolator.cu:526-528)
+  float* ffix = nullptr;
+  LC2_CUDA(cudaMalloc(&ffix, sizeof(float) * c->nf));
+  Free guard2{ffix};
+  LC2_CUDA(cudaMemcpyAsync(ffix, fixed, sizeof(float) * c->nf, cudaMemcpyHostToDevice, c->stream));
+  lc2::Xform id{};
+  {
+    float ident[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    float ident2[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    build_xform(c->warp_nd, c->virt, c->cfg.fixed, c->warp_nd == 2 ? ident2 : ident, &id);
+  }
+  c->h_xf[0] = id;
+  LC2_CUDA(cudaMemcpyAsync(c->d_xf, c->h_xf, sizeof(lc2::Xform), cudaMemcpyHostToDevice, c->stream));
+  float* vfix = c->d_scratch;  // slot 0 as temporary
+  LC2_TRY(launch_warp(c, c->warp_nd, ffix, LC2_STORE_F32, c->cfg.fixed, c->d_xf, 0, 1, vfix, c->nv));
+  if (c->cfg.high_res_is_moving) {
+    LC2_TRY(convert_to_storage(c, vfix, c->d_static, c->nv, storage));
+  } else {
+    LC2_CUDA(cudaMemcpyAsync(c->d_static, vfix, sizeof(float) * c->nv, cudaMemcpyDeviceToDevice,
+                             c->stream));
+    LC2_TRY(launch_sobel(c, (const float*)c->d_static, c->d_gstatic, 1, 0));
+  }
+  LC2_CUDA(cudaStreamSynchronize(c->stream));
+
+  // fixed-point scales and thresholds
+  const float tiny = 1e-30f;
+  float umax = c->cfg.high_res_is_moving ? fmax : mmax;
+  float hmax = c->cfg.high_res_is_moving ? mmax : fmax;
+  // Sobel magnitude bound: sum |taps| per component (8 in 2D, 32 in 3D)
+  float gmax = (c->lc2_nd == 3) ? std::sqrt(3.0f) * 32.0f * hmax : std::sqrt(2.0f) * 8.0f * hmax;
+  c->vmax_u = std::max(umax, tiny);
+  c->vmax_m = std::max(hmax, tiny);
+  c->vmax_g = std::max(gmax, tiny);
+  const float two_b = std::ldexp(1.0f, c->qbits);
+  lc2::MomentParams& P = c->mp;
+  P.vx = c->virt.dim[0];
+  P.vy = c->virt.dim[1];
+  P.vz = c->virt.dim[2];
+  P.r = c->cfg.patch_size;
+  P.n = c->n;
+  P.qu = two_b / c->vmax_u;
+  P.qm = two_b / c->vmax_m;
+  P.qg = two_b / c->vmax_g;
+  const long double n = c->n;
+  P.thr_var = floor_clamp(1e-6L * n * (n - 1) * (long double)P.qu * (long double)P.qu);
+  P.thr_m = floor_clamp(1e-12L * n * (n - 1) * (long double)P.qm * (long double)P.qm);
+  P.thr_g = floor_clamp(1e-12L * n * (n - 1) * (long double)P.qg * (long double)P.qg);
+  P.sig_scale = (float)(1.0L / ((long double)P.qu * std::sqrt(n * (n - 1))));
+  P.sum_scale = std::ldexp(1.0f, 29) / c->vmax_u;
+  c->ready = true;
+  return LC2_OK;
+}
+
+int lc2_stage_transforms(lc2_context* c, const float* matrices, int count) {
+  g_err.clear();
+  LC2_TRY(check_ctx(c));
+  if (count < 0 || (count > 0 && !matrices)) return fail(LC2_ERR_INVALID_ARGUMENT, "bad transforms");
+  LC2_TRY(select_device(c));
+  LC2_TRY(ensure_capacity(c, count));
+  const int mf = matrix_floats(c);
+  for (int k = 0; k < count; ++k) {
+    const float* m = matrices + (size_t)k * mf;
+    for (int i = 0; i < mf; ++i)
+      if (!std::isfinite(m[i])) return fail(LC2_ERR_INVALID_ARGUMENT, "transform %d has NaN/Inf", k);
+    build_xform(c->warp_nd, c->virt, c->cfg.moving, m, &c->h_xf[k]);
+  }
+  if (count > 0)
+    LC2_CUDA(cudaMemcpyAsync(c->d_xf, c->h_xf, sizeof(lc2::Xform) * count, cudaMemcpyHostToDevice,
+                             c->stream));
+  c->staged = count;
+  return LC2_OK;
+}
+
+int lc2_launch_staged(lc2_context* c, int count) {
+  LC2_TRY(check_ctx(c));
+  if (count < 0 || count > c->staged)
+    return fail(LC2_ERR_INVALID_ARGUMENT, "launch of %d transforms but %d staged", count, c->staged);
+  if (count == 0) return LC2_OK;
+  LC2_TRY(select_device(c));
+  LC2_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2 * count, c->stream));
+  for (int k0 = 0; k0 < count; k0 += c->slots) {
+    int cnt = std::min(c->slots, count - k0);
+    LC2_TRY(launch_group(c, k0, cnt, nullptr, nullptr));
+  }
+  lc2::k_finalize<<<(count + 127) / 128, 128, 0, c->stream>>>(c->d_acc, count, c->d_out);
+  ++c->launches;
+  LC2_CUDA(cudaGetLastError());
+  return LC2_OK;
+}
+
+int lc2_fetch_results(lc2_context* c, double* out, int count) {
+  LC2_TRY(check_ctx(c));
+  if (count < 0 || count > c->staged || (count > 0 && !out))
+    return fail(LC2_ERR_INVALID_ARGUMENT, "bad result request");
+  LC2_TRY(select_device(c));
+  if (count > 0)
+    LC2_CUDA(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(double) * count, cudaMemcpyDeviceToHost,
+                             c->stream));
+  LC2_CUDA(cudaStreamSynchronize(c->stream));
+  if (count > 0) std::memcpy(out, c->h_out, sizeof(double) * count);
+  return LC2_OK;
+}
+
+int lc2_evaluate_batch(lc2_context* c, const float* matrices, int count, double* out) {
+  LC2_TRY(lc2_stage_transforms(c, matrices, count));
+  LC2_TRY(lc2_launch_staged(c, count));
+  return lc2_fetch_results(c, out, count);
+}
+
+int lc2_evaluate(lc2_context* c, const float* matrix, double* out) {
+  if (!out) return fail(LC2_ERR_INVALID_ARGUMENT, "null output");
+  return lc2_evaluate_batch(c, matrix, 1, out);
+}
+
+int lc2_evaluate_fields(lc2_context* c, const float* matrix, double* lc2_out, float* U, float* M,
+                        float* G, float* sigma, float* measure) {
+  LC2_TRY(lc2_stage_transforms(c, matrix, 1));
+  LC2_TRY(select_device(c));
+  const size_t nv = c->nv;
+  float* osig = nullptr;
+  float* omeas = nullptr;
+  LC2_CUDA(cudaMalloc(&osig, sizeof(float) * nv * 3));
+  struct Free {
+    float* p;
+    ~Free() { cudaFree(p); }
+  } guard{osig};
+  omeas = osig + nv;
+  float* tmp = osig + 2 * nv;
+  LC2_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2, c->stream));
+  LC2_TRY(launch_group(c, 0, 1, osig, omeas));
+  lc2::k_finalize<<<1, 32, 0, c->stream>>>(c->d_acc, 1, c->d_out);
+  ++c->launches;
+  LC2_CUDA(cudaGetLastError());
+  float* w = c->d_scratch;
+  const bool hrm = c->cfg.high_res_is_moving != 0;
+  const float* dU = hrm ? nullptr : w;
+  const float* dM = hrm ? w : (const float*)c->d_static;
+  const float* dG = hrm ? c->d_scratch + (size_t)c->slots * nv : c->d_gstatic;
+  if (U) {
+    if (hrm) {
+      LC2_TRY(to_float(c, c->d_static, tmp, nv, c->cfg.storage));
+      dU = tmp;
+    }
+    LC2_CUDA(cudaMemcpyAsync(U, dU, sizeof(float) * nv, cudaMemcpyDeviceToHost, c->stream));
+  }
+  if (M) LC2_CUDA(cudaMemcpyAsync(M, dM, sizeof(float) * nv, cudaMemcpyDeviceToHost, c->stream));
+  if (G) LC2_CUDA(cudaMemcpyAsync(G, dG, sizeof(float) * nv, cudaMemcpyDeviceToHost, c->stream));
+  if (sigma) LC2_CUDA(cudaMemcpyAsync(sigma, osig, sizeof(float) * nv, cudaMemcpyDeviceToHost, c->stream));
+  if (measure)
+    LC2_CUDA(cudaMemcpyAsync(measure, omeas, sizeof(float) * nv, cudaMemcpyDeviceToHost, c->stream));
+  LC2_CUDA(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  LC2_CUDA(cudaStreamSynchronize(c->stream));
+  if (lc2_out) *lc2_out = c->h_out[0];
+  return LC2_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Transform builders (host)
+// ---------------------------------------------------------------------------
+
+int lc2_affine_3d(const float rot[3], const float trans[3], const float scale[3],
+                  const float shear[3], const float center[3], const float shift[3],
+                  float out[16]) {
+  if (!rot || !trans || !scale || !shear || !center || !shift || !out)
+    return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  const double d2r = 3.14159265358979323846 / 180.0;
+  double c[3], s[3];
+  for (int a = 0; a < 3; ++a) {
+    c[a] = std::cos((double)rot[a] * d2r);
+    s[a] = std::sin((double)rot[a] * d2r);
+  }
+  double Rx[3][3] = {{1, 0, 0}, {0, c[0], -s[0]}, {0, s[0], c[0]}};
+  double Ry[3][3] = {{c[1], 0, s[1]}, {0, 1, 0}, {-s[1], 0, c[1]}};
+  double Rz[3][3] = {{c[2], -s[2], 0}, {s[2], c[2], 0}, {0, 0, 1}};
+  double ShS[3][3] = {{scale[0], (double)shear[0] * scale[1], (double)shear[1] * scale[2]},
+                      {0, scale[1], (double)shear[2] * scale[2]},
+                      {0, 0, scale[2]}};
+  auto mul = [](const double A[3][3], const double B[3][3], double C[3][3]) {
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        C[i][j] = 0;
+        for (int k = 0; k < 3; ++k) C[i][j] += A[i][k] * B[k][j];
+      }
+  };
+  double T1[3][3], T2[3][3], L[3][3];
+  mul(Rx, ShS, T1);
+  mul(Ry, T1, T2);
+  mul(Rz, T2, L);
+  for (int i = 0; i < 3; ++i) {
+    double t = (double)center[i] + trans[i];
+    for (int k = 0; k < 3; ++k) t += L[i][k] * ((double)shift[k] - center[k]);
+    for (int j = 0; j < 3; ++j) out[4 * i + j] = (float)L[i][j];
+    out[4 * i + 3] = (float)t;
+  }
+  out[12] = out[13] = out[14] = 0.0f;
+  out[15] = 1.0f;
+  return LC2_OK;
+}
+
+int lc2_affine_2d(float rot, const float trans[2], const float scale[2], float shear,
+                  const float center[2], const float shift[2], float out[9]) {
+  if (!trans || !scale || !center || !shift || !out) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  const double d2r = 3.14159265358979323846 / 180.0;
+  double c = std::cos((double)rot * d2r), s = std::sin((double)rot * d2r);
+  double L[2][2] = {{c * scale[0], scale[1] * (c * shear - s)}, {s * scale[0], scale[1] * (s * shear + c)}};
+  for (int i = 0; i < 2; ++i) {
+    double t = (double)center[i] + trans[i];
+    for (int k = 0; k < 2; ++k) t += L[i][k] * ((double)shift[k] - center[k]);
+    out[3 * i + 0] = (float)L[i][0];
+    out[3 * i + 1] = (float)L[i][1];
+    out[3 * i + 2] = (float)t;
+  }
+  out[6] = out[7] = 0.0f;
+  out[8] = 1.0f;
+  return LC2_OK;
+}
+
+int lc2_invert_affine_3d(const float in[16], float out[16]) {
+  if (!in || !out) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  double a[3][3], t[3];
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) a[i][j] = in[4 * i + j];
+    t[i] = in[4 * i + 3];
+  }
+  double det = a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) -
+               a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+               a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+  if (det == 0.0 || !std::isfinite(det)) return fail(LC2_ERR_SINGULAR, "singular transform");
+  double inv[3][3];
+  inv[0][0] = (a[1][1] * a[2][2] - a[1][2] * a[2][1]) / det;
+  inv[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) / det;
+  inv[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) / det;
+  inv[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) / det;
+  inv[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) / det;
+  inv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) / det;
+  inv[2][0] = (a[1][0] * a[2][1] - a[1][1] * a[2][0]) / det;
+  inv[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) / det;
+  inv[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) / det;
+  for (int i = 0; i < 3; ++i) {
+    double ti = 0;
+    for (int j = 0; j < 3; ++j) {
+      out[4 * i + j] = (float)inv[i][j];
+      ti -= inv[i][j] * t[j];
+    }
+    out[4 * i + 3] = (float)ti;
+  }
+  out[12] = out[13] = out[14] = 0.0f;
+  out[15] = 1.0f;
+  return LC2_OK;
+}
+
+}  // extern "C"

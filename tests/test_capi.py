@@ -1,0 +1,69 @@
+"""CPU checks of the C ABI library: it builds, loads, exports every symbol
+include/lc2.h declares, and rejects bad arguments before touching a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from lc2registration_gb300 import capi
+from lc2registration_gb300.geometry import Geometry
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", fn)).read()
+            txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+            names |= set(re.findall(r"\b(lc2_[a-z0-9_]+)\s*\(", txt))
+    return sorted(names)
+
+
+def test_library_loads_and_exports_all_declared_symbols():
+    lib = capi.load()
+    declared = _declared()
+    assert declared, "no declarations found"
+    missing = [n for n in declared if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(declared) == set(capi.EXPORTED)
+
+
+def test_version_and_error_string():
+    lib = capi.load()
+    assert b"sm_103a" in lib.lc2_version()
+    assert isinstance(lib.lc2_last_error(), bytes)
+
+
+def test_rejects_bad_config_without_gpu():
+    g = Geometry((32, 32, 1), (1, 1, 1), (0, 0, 0))
+    with pytest.raises(capi.LC2Error) as e:
+        capi.Context("2D", g, g, (1.0, 1.0), patch_size=0)
+    assert e.value.status == 6  # unsupported patch size
+    with pytest.raises(capi.LC2Error) as e:
+        capi.Context("3D", Geometry((8, 8, 8), (1, 1, 1), (0, 0, 0)), g, (1, 1, 1), patch_size=7)
+    assert e.value.status == 6
+    bad = Geometry((32, 32, 1), (0.0, 1, 1), (0, 0, 0))
+    with pytest.raises(capi.LC2Error) as e:
+        capi.Context("2D", bad, g, (1.0, 1.0), patch_size=3)
+    assert e.value.status == 1
+    lib = capi.load()
+    h = ctypes.c_void_p()
+    assert lib.lc2_create(None, ctypes.byref(h)) == 1
+
+
+def test_singular_inverse_rejected():
+    with pytest.raises(capi.LC2Error) as e:
+        capi.invert_affine_3d(np.zeros((4, 4), dtype=np.float32))
+    assert e.value.status == 5
+
+
+def test_null_context_calls_fail_cleanly():
+    lib = capi.load()
+    out = ctypes.c_double()
+    m = (ctypes.c_float * 16)()
+    assert lib.lc2_evaluate(None, m, ctypes.byref(out)) != 0
+    assert lib.lc2_destroy(None) == 0
