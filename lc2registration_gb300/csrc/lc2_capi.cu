@@ -13,6 +13,7 @@
 
 #include "../../include/lc2.h"
 #include "lc2_kernels.cuh"
+#include "lc2_fused.cuh"
 
 namespace {
 
@@ -74,7 +75,12 @@ struct lc2_context {
   int staged = 0;
 
   lc2::MomentParams mp{};
+  lc2::FusedParams fp{};
   float vmax_u = 0, vmax_m = 0, vmax_g = 0;
+  // static ultrasound (HighResolutionModality: Moving): weighting factor per
+  // voxel and its exact fixed-point sum
+  float* d_sigma = nullptr;
+  long long sigma_sum = -1;
 
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
@@ -316,8 +322,10 @@ void choose_zchunks(const lc2_context* c, int cnt, lc2::MomentParams& P) {
   P.nzchunks = (v.dim[2] + P.zchunk - 1) / P.zchunk;
 }
 
-// Enqueue the evaluation of staged transforms [k0, k0 + cnt), cnt <= slots.
-int launch_group(lc2_context* c, int k0, int cnt, float* osig, float* omeas) {
+// Generic path: resample -> Sobel -> moments through global scratch. Used for
+// a resampled ultrasound (HighResolutionModality: Fixed), for the one-time
+// weighting-factor precompute and for the diagnostic field dumps.
+int launch_group_generic(lc2_context* c, int k0, int cnt, float* osig, float* omeas) {
   const size_t nv = c->nv;
   lc2::MomentParams P = c->mp;
   choose_zchunks(c, cnt, P);
@@ -344,6 +352,66 @@ int launch_group(lc2_context* c, int k0, int cnt, float* osig, float* omeas) {
                                 k0, cnt, osig, omeas);
   return launch_moments_nd<2>(c, w, LC2_STORE_F32, (const float*)c->d_static, c->d_gstatic, P, k0,
                               cnt, osig, omeas);
+}
+
+// Tile height of the fused kernel: 16 rows while the shared-memory rings fit.
+int fused_ty(const lc2_context* c) { return (c->lc2_nd == 3 && c->cfg.patch_size > 4) ? 8 : 16; }
+
+template <int ND, int WND, typename T, int TY>
+int launch_fused_t(lc2_context* c, int k0, int cnt, float* omeas) {
+  lc2::FusedParams P = c->fp;
+  const lc2_geometry& v = c->virt;
+  const int ntx = (v.dim[0] + 31) / 32, nty = (v.dim[1] + TY - 1) / TY;
+  P.ntx = ntx;
+  int nz = 1;
+  if (ND == 3) {
+    long long ctas = (long long)ntx * nty * cnt;
+    nz = (int)std::max<long long>(1, (4LL * 152 + ctas - 1) / ctas);
+    nz = std::min(nz, std::max(1, v.dim[2] / (4 * P.r + 4)));
+    nz = std::min(nz, 65535);
+  }
+  P.zchunk = (ND == 3) ? (v.dim[2] + nz - 1) / nz : 1;
+  nz = (ND == 3) ? (v.dim[2] + P.zchunk - 1) / P.zchunk : 1;
+  const size_t smem = lc2::fused_smem_bytes(P.r, TY, ND);
+  auto kern = lc2::k_fused<ND, WND, T, T, TY>;
+  LC2_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid(cnt, ntx * nty, nz);
+  TimerScope ts(c, K_MOMENTS);
+  kern<<<grid, 32 * TY, smem, c->stream>>>((const T*)c->d_moving, (const T*)c->d_static, c->d_sigma,
+                                           P, c->d_xf, k0, c->d_acc, omeas);
+  ++c->launches;
+  LC2_CUDA(cudaGetLastError());
+  return LC2_OK;
+}
+
+template <typename T>
+int launch_fused_ty(lc2_context* c, int k0, int cnt, float* omeas) {
+  if (c->lc2_nd == 3) {
+    if (fused_ty(c) == 16) return launch_fused_t<3, 3, T, 16>(c, k0, cnt, omeas);
+    return launch_fused_t<3, 3, T, 8>(c, k0, cnt, omeas);
+  }
+  if (c->warp_nd == 3) return launch_fused_t<2, 3, T, 16>(c, k0, cnt, omeas);
+  return launch_fused_t<2, 2, T, 16>(c, k0, cnt, omeas);
+}
+
+int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
+  if (c->cfg.storage == LC2_STORE_F16) return launch_fused_ty<__half>(c, k0, cnt, omeas);
+  if (c->cfg.storage == LC2_STORE_BF16) return launch_fused_ty<__nv_bfloat16>(c, k0, cnt, omeas);
+  return launch_fused_ty<float>(c, k0, cnt, omeas);
+}
+
+// Enqueue the evaluation of staged transforms [k0, k0 + cnt).
+int launch_group(lc2_context* c, int k0, int cnt) {
+  if (c->cfg.high_res_is_moving) return launch_fused(c, k0, cnt, nullptr);
+  return launch_group_generic(c, k0, cnt, nullptr, nullptr);
+}
+
+int launch_finalize(lc2_context* c, int count) {
+  lc2::k_finalize<<<(count + 127) / 128, 128, 0, c->stream>>>(
+      c->d_acc, count, c->d_out, c->cfg.high_res_is_moving ? c->sigma_sum : -1LL);
+  ++c->launches;
+  LC2_CUDA(cudaGetLastError());
+  return LC2_OK;
 }
 
 int matrix_floats(const lc2_context* c) { return c->warp_nd == 2 ? 9 : 16; }
@@ -447,6 +515,8 @@ int lc2_create(const lc2_config* cfg, lc2_context** out) {
                    c->nv * (cfg->high_res_is_moving ? elem_size(cfg->storage) : sizeof(float)));
   if (e == cudaSuccess && !cfg->high_res_is_moving)
     e = cudaMalloc(&c->d_gstatic, c->nv * sizeof(float));
+  if (e == cudaSuccess && cfg->high_res_is_moving)
+    e = cudaMalloc(&c->d_sigma, c->nv * sizeof(float));
   if (e != cudaSuccess) {
     lc2_destroy(c);
     return fail(LC2_ERR_OUT_OF_MEMORY, "device allocation: %s", cudaGetErrorString(e));
@@ -469,6 +539,7 @@ int lc2_destroy(lc2_context* c) {
   cudaFree(c->d_moving);
   cudaFree(c->d_static);
   cudaFree(c->d_gstatic);
+  cudaFree(c->d_sigma);
   cudaFree(c->d_scratch);
   cudaFree(c->d_xf);
   cudaFree(c->d_acc);
@@ -602,6 +673,41 @@ int lc2_set_images(lc2_context* c, const float* fixed, const float* moving) {
   P.thr_g = floor_clamp(1e-12L * n * (n - 1) * (long double)P.qg * (long double)P.qg);
   P.sig_scale = (float)(1.0L / ((long double)P.qu * std::sqrt(n * (n - 1))));
   P.sum_scale = std::ldexp(1.0f, 29) / c->vmax_u;
+  // fused-kernel parameters
+  lc2::FusedParams& F = c->fp;
+  F.vx = P.vx;
+  F.vy = P.vy;
+  F.vz = P.vz;
+  F.mx = c->cfg.moving.dim[0];
+  F.my = c->cfg.moving.dim[1];
+  F.mz = c->cfg.moving.dim[2];
+  F.r = P.r;
+  F.n = P.n;
+  F.qu = P.qu;
+  F.qm = P.qm;
+  F.qg = P.qg;
+  F.thr_m = P.thr_m;
+  F.thr_g = P.thr_g;
+  F.sig_scale = P.sig_scale;
+  F.sum_scale = P.sum_scale;
+  if (c->cfg.high_res_is_moving) {
+    // the ultrasound is static: its weighting factor per voxel and their sum,
+    // once, with the generic moments kernel on M = G = 0
+    float* zero = c->d_scratch;
+    LC2_CUDA(cudaMemsetAsync(zero, 0, sizeof(float) * c->nv, c->stream));
+    LC2_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2, c->stream));
+    lc2::MomentParams Q = P;
+    choose_zchunks(c, 1, Q);
+    Q.u_stride = Q.m_stride = Q.g_stride = 0;
+    if (c->lc2_nd == 3)
+      LC2_TRY(launch_moments_nd<3>(c, c->d_static, storage, zero, zero, Q, 0, 1, c->d_sigma, nullptr));
+    else
+      LC2_TRY(launch_moments_nd<2>(c, c->d_static, storage, zero, zero, Q, 0, 1, c->d_sigma, nullptr));
+    unsigned long long sums[2] = {0, 0};
+    LC2_CUDA(cudaMemcpyAsync(sums, c->d_acc, sizeof(sums), cudaMemcpyDeviceToHost, c->stream));
+    LC2_CUDA(cudaStreamSynchronize(c->stream));
+    c->sigma_sum = (long long)sums[1];
+  }
   c->ready = true;
   return LC2_OK;
 }
@@ -633,14 +739,14 @@ int lc2_launch_staged(lc2_context* c, int count) {
   if (count == 0) return LC2_OK;
   LC2_TRY(select_device(c));
   LC2_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2 * count, c->stream));
-  for (int k0 = 0; k0 < count; k0 += c->slots) {
-    int cnt = std::min(c->slots, count - k0);
-    LC2_TRY(launch_group(c, k0, cnt, nullptr, nullptr));
+  // the fused path keeps nothing per transform on the device, so one launch
+  // covers the whole batch; the generic path is bounded by its scratch slots
+  const int group = c->cfg.high_res_is_moving ? count : c->slots;
+  for (int k0 = 0; k0 < count; k0 += group) {
+    int cnt = std::min(group, count - k0);
+    LC2_TRY(launch_group(c, k0, cnt));
   }
-  lc2::k_finalize<<<(count + 127) / 128, 128, 0, c->stream>>>(c->d_acc, count, c->d_out);
-  ++c->launches;
-  LC2_CUDA(cudaGetLastError());
-  return LC2_OK;
+  return launch_finalize(c, count);
 }
 
 int lc2_fetch_results(lc2_context* c, double* out, int count) {
@@ -682,10 +788,21 @@ int lc2_evaluate_fields(lc2_context* c, const float* matrix, double* lc2_out, fl
   omeas = osig + nv;
   float* tmp = osig + 2 * nv;
   LC2_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2, c->stream));
-  LC2_TRY(launch_group(c, 0, 1, osig, omeas));
-  lc2::k_finalize<<<1, 32, 0, c->stream>>>(c->d_acc, 1, c->d_out);
-  ++c->launches;
-  LC2_CUDA(cudaGetLastError());
+  if (c->cfg.high_res_is_moving) {
+    // LC2 and measures from the fused kernel; M and G from the generic
+    // resample/Sobel kernels; sigma is the precomputed static map
+    LC2_TRY(launch_fused(c, 0, 1, omeas));
+    LC2_TRY(launch_finalize(c, 1));
+    float* w0 = c->d_scratch;
+    LC2_TRY(launch_warp(c, c->warp_nd, c->d_moving, c->cfg.storage, c->cfg.moving, c->d_xf, 0, 1,
+                        w0, nv));
+    LC2_TRY(launch_sobel(c, w0, c->d_scratch + (size_t)c->slots * nv, 1, nv));
+    LC2_CUDA(cudaMemcpyAsync(osig, c->d_sigma, sizeof(float) * nv, cudaMemcpyDeviceToDevice,
+                             c->stream));
+  } else {
+    LC2_TRY(launch_group_generic(c, 0, 1, osig, omeas));
+    LC2_TRY(launch_finalize(c, 1));
+  }
   float* w = c->d_scratch;
   const bool hrm = c->cfg.high_res_is_moving != 0;
   const float* dU = hrm ? nullptr : w;

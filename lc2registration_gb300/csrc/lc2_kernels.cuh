@@ -525,11 +525,9 @@ __global__ void __launch_bounds__(kNT) k_moments(const TU* __restrict__ Ubase,
                   s.y64[py + o], s.y64[2 * py + o], s.y64[3 * py + o], s.y64[4 * py + o],
                   s.y64[5 * py + o], sg, ms);
       add_sums(P, sg, ms, acc_m, acc_s);
-      if (out_sigma) {
-        size_t gi = (size_t)y * P.vx + x;
-        out_sigma[gi] = sg;
-        out_measure[gi] = ms;
-      }
+      const size_t gi = (size_t)y * P.vx + x;
+      if (out_sigma) out_sigma[gi] = sg;
+      if (out_measure) out_measure[gi] = ms;
     }
     flush_sums(acc_m, acc_s, acc + 2 * (size_t)(k0 + slot));
     return;
@@ -601,11 +599,9 @@ __global__ void __launch_bounds__(kNT) k_moments(const TU* __restrict__ Ubase,
                   s.y64[py + o], s.y64[2 * py + o], s.y64[3 * py + o], s.y64[4 * py + o],
                   s.y64[5 * py + o], sg, ms);
       add_sums(P, sg, ms, acc_m, acc_s);
-      if (out_sigma) {
-        size_t gi = ((size_t)z * P.vy + y) * P.vx + x;
-        out_sigma[gi] = sg;
-        out_measure[gi] = ms;
-      }
+      const size_t gi = ((size_t)z * P.vy + y) * P.vx + x;
+      if (out_sigma) out_sigma[gi] = sg;
+      if (out_measure) out_measure[gi] = ms;
     }
     // the next z-phase overwrites the z planes only; x/y planes are rewritten
     // after the next barrier, so no extra barrier is needed here
@@ -614,11 +610,14 @@ __global__ void __launch_bounds__(kNT) k_moments(const TU* __restrict__ Ubase,
 }
 
 // LC2 = sum(measure) / sum(sigma); 0 when NaN/Inf (cu_lc2_3d.cu:1189-1191).
+// sigma_sum >= 0: the weighting-factor sum is static (precomputed), else it
+// is taken from the accumulator.
 __global__ void k_finalize(const unsigned long long* __restrict__ acc, int count,
-                           double* __restrict__ out) {
+                           double* __restrict__ out, long long sigma_sum) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
-  double m = (double)(long long)acc[2 * k], s = (double)(long long)acc[2 * k + 1];
+  double m = (double)(long long)acc[2 * k];
+  double s = sigma_sum >= 0 ? (double)sigma_sum : (double)(long long)acc[2 * k + 1];
   double v = m / s;
   if (isnan(v) || isinf(v)) v = 0.0;
   out[k] = v;
