@@ -273,7 +273,7 @@ def main():
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "moments_traffic.json")
+    tfile = os.path.join(ROOT, "profiles", "k_fused_traffic.json")
     if os.path.exists(tfile):
         try:
             traffic = json.load(open(tfile)).get("bytes_per_launch_scaled")
@@ -323,7 +323,7 @@ def main():
             "config": config_dict(args, case),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_moments", "kernel_ms_per_launch": mom_ms / max(1, mom_launches),
+                         "kernel": "k_fused", "kernel_ms_per_launch": mom_ms / max(1, mom_launches),
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
             "kernels_ms_per_step": {k: v[0] for k, v in kt.items()},
             "cpu_baseline": cpu,

@@ -119,6 +119,13 @@ int lc2_evaluate_fields(lc2_context* ctx, const float* matrix, double* lc2_out, 
  * accounting for benchmarks). */
 long long lc2_launch_count(const lc2_context* ctx);
 
+/* Tuning options (lc2_set_option). LC2_OPTION_TILE_ROWS: output rows per
+ * tile of the fused 3D kernel, 16 (one CTA per SM) or 8 (two per SM); 0 =
+ * automatic. No counterpart in the reference (its block sizes are arguments
+ * of CalculateGradient / GetSimilarityMetric, src/cu_LC2/cu_lc2_3d.cuh:36-41). */
+enum { LC2_OPTION_TILE_ROWS = 1 };
+int lc2_set_option(lc2_context* ctx, int option, int value);
+
 /* Per-kernel device timing with CUDA events on the context stream (off by
  * default). lc2_kernel_times synchronises, returns the summed milliseconds
  * and launch counts of the resampling, Sobel and moments kernels since the

@@ -15,8 +15,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(OUT_DIR, "liblc2.so")
-SOURCES = ["lc2_capi.cu"]
-DEPS = ["lc2_capi.cu", "lc2_kernels.cuh"]
+SOURCES = ["lc2_capi.cu", "lc2_fused_f32.cu", "lc2_fused_f16.cu", "lc2_fused_bf16.cu"]
+DEPS = SOURCES + ["lc2_kernels.cuh", "lc2_fused.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -36,15 +36,25 @@ def needs_build() -> bool:
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile each translation unit in parallel, then link liblc2.so."""
     if not force and not needs_build():
         return LIB_PATH
     os.makedirs(OUT_DIR, exist_ok=True)
+    common = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+              "-I", os.path.join(ROOT, "include")]
+    procs, objs = [], []
+    for src in SOURCES:
+        obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
+        cmd = common + ["-c", os.path.join(CSRC, src), "-o", obj]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        procs.append((src, subprocess.Popen(cmd)))
+        objs.append(obj)
+    failed = [src for src, p in procs if p.wait() != 0]
+    if failed:
+        raise RuntimeError(f"nvcc failed on {failed}")
     tmp = LIB_PATH + ".tmp"
-    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-           "-I", os.path.join(ROOT, "include"), "-o", tmp] + [os.path.join(CSRC, s) for s in SOURCES]
-    if verbose:
-        print(" ".join(cmd), file=sys.stderr)
-    subprocess.run(cmd, check=True)
+    subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp] + objs, check=True)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 

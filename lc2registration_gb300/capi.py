@@ -25,6 +25,7 @@ STATUS_NAMES = {
     6: "LC2_ERR_UNSUPPORTED",
 }
 MODES = {"2D": 0, "3D": 1, "2DTo3D": 2}
+OPTION_TILE_ROWS = 1
 STORAGE = {"f32": 0, "f16": 1, "bf16": 2}
 
 # Every symbol include/lc2.h declares (checked by the test suite).
@@ -32,7 +33,7 @@ EXPORTED = [
     "lc2_create", "lc2_destroy", "lc2_set_images", "lc2_virtual_dims", "lc2_evaluate",
     "lc2_evaluate_batch", "lc2_stage_transforms", "lc2_launch_staged", "lc2_fetch_results",
     "lc2_get_stream", "lc2_set_stream", "lc2_evaluate_fields", "lc2_launch_count",
-    "lc2_enable_kernel_timing", "lc2_kernel_times",
+    "lc2_enable_kernel_timing", "lc2_kernel_times", "lc2_set_option",
     "lc2_affine_3d", "lc2_affine_2d", "lc2_invert_affine_3d", "lc2_last_error", "lc2_version",
 ]
 
@@ -87,6 +88,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "lc2_evaluate_fields": ([vp, _fp, _dp, _fp, _fp, _fp, _fp, _fp], ctypes.c_int),
         "lc2_launch_count": ([vp], ctypes.c_longlong),
         "lc2_enable_kernel_timing": ([vp, ctypes.c_int], ctypes.c_int),
+        "lc2_set_option": ([vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "lc2_kernel_times": ([vp, _dp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
         "lc2_affine_3d": ([_fp, _fp, _fp, _fp, _fp, _fp, _fp], ctypes.c_int),
         "lc2_affine_2d": ([ctypes.c_float, _fp, _fp, ctypes.c_float, _fp, _fp, _fp], ctypes.c_int),
@@ -213,6 +215,9 @@ class Context:
 
     def launch_count(self) -> int:
         return int(self._lib.lc2_launch_count(self._h))
+
+    def set_option(self, option: int, value: int):
+        _check(self._lib.lc2_set_option(self._h, int(option), int(value)))
 
     def enable_kernel_timing(self, on: bool = True):
         _check(self._lib.lc2_enable_kernel_timing(self._h, int(bool(on))))

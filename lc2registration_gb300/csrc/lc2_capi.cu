@@ -81,6 +81,7 @@ struct lc2_context {
   // voxel and its exact fixed-point sum
   float* d_sigma = nullptr;
   long long sigma_sum = -1;
+  int tile_rows = 0;  // fused kernel tile height (0 = automatic)
 
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
@@ -94,6 +95,23 @@ struct lc2_context {
   };
   std::vector<Timed> timed;
 };
+
+namespace lc2 {
+// LC2 = sum(measure) / sum(sigma); 0 when NaN/Inf (cu_lc2_3d.cu:1189-1191).
+// sigma_sum >= 0: the weighting-factor sum is static (precomputed), else it
+// is taken from the accumulator.
+__global__ void k_finalize(const unsigned long long* __restrict__ acc, int count,
+                           double* __restrict__ out, long long sigma_sum) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  double m = (double)(long long)acc[2 * k];
+  double s = sigma_sum >= 0 ? (double)sigma_sum : (double)(long long)acc[2 * k + 1];
+  double v = m / s;
+  if (isnan(v) || isinf(v)) v = 0.0;
+  out[k] = v;
+}
+
+}  // namespace lc2
 
 namespace {
 
@@ -354,50 +372,35 @@ int launch_group_generic(lc2_context* c, int k0, int cnt, float* osig, float* om
                               cnt, osig, omeas);
 }
 
-// Tile height of the fused kernel: 16 rows while the shared-memory rings fit.
-int fused_ty(const lc2_context* c) { return (c->lc2_nd == 3 && c->cfg.patch_size > 4) ? 8 : 16; }
-
-template <int ND, int WND, typename T, int TY>
-int launch_fused_t(lc2_context* c, int k0, int cnt, float* omeas) {
-  lc2::FusedParams P = c->fp;
-  const lc2_geometry& v = c->virt;
-  const int ntx = (v.dim[0] + 31) / 32, nty = (v.dim[1] + TY - 1) / TY;
-  P.ntx = ntx;
-  int nz = 1;
-  if (ND == 3) {
-    long long ctas = (long long)ntx * nty * cnt;
-    nz = (int)std::max<long long>(1, (4LL * 152 + ctas - 1) / ctas);
-    nz = std::min(nz, std::max(1, v.dim[2] / (4 * P.r + 4)));
-    nz = std::min(nz, 65535);
-  }
-  P.zchunk = (ND == 3) ? (v.dim[2] + nz - 1) / nz : 1;
-  nz = (ND == 3) ? (v.dim[2] + P.zchunk - 1) / P.zchunk : 1;
-  const size_t smem = lc2::fused_smem_bytes(P.r, TY, ND);
-  auto kern = lc2::k_fused<ND, WND, T, T, TY>;
-  LC2_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid(cnt, ntx * nty, nz);
-  TimerScope ts(c, K_MOMENTS);
-  kern<<<grid, 32 * TY, smem, c->stream>>>((const T*)c->d_moving, (const T*)c->d_static, c->d_sigma,
-                                           P, c->d_xf, k0, c->d_acc, omeas);
-  ++c->launches;
-  LC2_CUDA(cudaGetLastError());
-  return LC2_OK;
-}
-
-template <typename T>
-int launch_fused_ty(lc2_context* c, int k0, int cnt, float* omeas) {
-  if (c->lc2_nd == 3) {
-    if (fused_ty(c) == 16) return launch_fused_t<3, 3, T, 16>(c, k0, cnt, omeas);
-    return launch_fused_t<3, 3, T, 8>(c, k0, cnt, omeas);
-  }
-  if (c->warp_nd == 3) return launch_fused_t<2, 3, T, 16>(c, k0, cnt, omeas);
-  return launch_fused_t<2, 2, T, 16>(c, k0, cnt, omeas);
-}
-
+// The fused kernel (static ultrasound): one launch for `cnt` transforms.
 int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
-  if (c->cfg.storage == LC2_STORE_F16) return launch_fused_ty<__half>(c, k0, cnt, omeas);
-  if (c->cfg.storage == LC2_STORE_BF16) return launch_fused_ty<__nv_bfloat16>(c, k0, cnt, omeas);
-  return launch_fused_ty<float>(c, k0, cnt, omeas);
+  lc2::FusedLaunch L;
+  L.mov = c->d_moving;
+  L.ust = c->d_static;
+  L.sig = c->d_sigma;
+  L.P = c->fp;
+  L.xf = c->d_xf;
+  L.k0 = k0;
+  L.cnt = cnt;
+  L.acc = c->d_acc;
+  L.out_measure = omeas;
+  L.nd = c->lc2_nd;
+  L.wnd = c->warp_nd;
+  L.tile_height = c->tile_rows > 0 ? c->tile_rows : 16;
+  L.stream = c->stream;
+  cudaError_t e;
+  {
+    TimerScope ts(c, K_MOMENTS);
+    if (c->cfg.storage == LC2_STORE_F16)
+      e = lc2::fused_launch<__half>(L);
+    else if (c->cfg.storage == LC2_STORE_BF16)
+      e = lc2::fused_launch<__nv_bfloat16>(L);
+    else
+      e = lc2::fused_launch<float>(L);
+  }
+  ++c->launches;
+  LC2_CUDA(e);
+  return LC2_OK;
 }
 
 // Enqueue the evaluation of staged transforms [k0, k0 + cnt).
@@ -571,6 +574,17 @@ int lc2_set_stream(lc2_context* c, void* stream) {
 
 long long lc2_launch_count(const lc2_context* c) { return c ? c->launches : 0; }
 
+int lc2_set_option(lc2_context* c, int option, int value) {
+  if (!c) return fail(LC2_ERR_INVALID_ARGUMENT, "null context");
+  if (option == LC2_OPTION_TILE_ROWS) {
+    if (value != 0 && value != 8 && value != 16)
+      return fail(LC2_ERR_INVALID_ARGUMENT, "tile rows must be 0, 8 or 16");
+    c->tile_rows = value;
+    return LC2_OK;
+  }
+  return fail(LC2_ERR_INVALID_ARGUMENT, "unknown option %d", option);
+}
+
 int lc2_enable_kernel_timing(lc2_context* c, int on) {
   if (!c) return fail(LC2_ERR_INVALID_ARGUMENT, "null context");
   c->timing = on != 0;
@@ -690,6 +704,9 @@ int lc2_set_images(lc2_context* c, const float* fixed, const float* moving) {
   F.thr_g = P.thr_g;
   F.sig_scale = P.sig_scale;
   F.sum_scale = P.sum_scale;
+  // limb split: every low limb's window sum (n+1 terms) stays below 2^30
+  F.kbits = 0;
+  while (((long long)(c->n + 1) << (F.kbits + 1)) <= (1LL << 30)) ++F.kbits;
   if (c->cfg.high_res_is_moving) {
     // the ultrasound is static: its weighting factor per voxel and their sum,
     // once, with the generic moments kernel on M = G = 0

@@ -1,0 +1,7 @@
+// Fused LC2 kernels for f32 storage (all patch radii), one translation unit
+// per storage type so the instantiations compile in parallel.
+#include "lc2_fused.cuh"
+
+namespace lc2 {
+LC2_DEFINE_FUSED_LAUNCH(float)
+}  // namespace lc2

@@ -609,20 +609,6 @@ __global__ void __launch_bounds__(kNT) k_moments(const TU* __restrict__ Ubase,
   flush_sums(acc_m, acc_s, acc + 2 * (size_t)(k0 + slot));
 }
 
-// LC2 = sum(measure) / sum(sigma); 0 when NaN/Inf (cu_lc2_3d.cu:1189-1191).
-// sigma_sum >= 0: the weighting-factor sum is static (precomputed), else it
-// is taken from the accumulator.
-__global__ void k_finalize(const unsigned long long* __restrict__ acc, int count,
-                           double* __restrict__ out, long long sigma_sum) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= count) return;
-  double m = (double)(long long)acc[2 * k];
-  double s = sigma_sum >= 0 ? (double)sigma_sum : (double)(long long)acc[2 * k + 1];
-  double v = m / s;
-  if (isnan(v) || isinf(v)) v = 0.0;
-  out[k] = v;
-}
-
 // float -> storage type conversion of a device buffer
 template <typename T>
 __global__ void k_convert(const float* __restrict__ in, T* __restrict__ out, size_t n) {
