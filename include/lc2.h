@@ -149,6 +149,34 @@ int lc2_affine_2d(float rotation, const float translation[2], const float scale[
  * LC2_ERR_SINGULAR when the determinant is 0. */
 int lc2_invert_affine_3d(const float in[16], float out[16]);
 
+/* Evaluation for callers that cannot allocate device memory: a host
+ * application whose allocator or memory pool owns the device heap, a
+ * real-time loop that must not allocate after start-up, a plug-in handed
+ * device buffers and nothing else. No counterpart in the reference.
+ *
+ * Inputs and output are the caller's device buffers: d_ultrasound is the
+ * ultrasound already on the virtual grid `virt` (float32, x fastest; the
+ * ultrasound is the fixed image, i.e. HighResolutionModality: Moving),
+ * d_moving the moving image with geometry `moving`, matrix the host-side
+ * virtual->moving matrix (3x3 in 2D mode, 4x4 otherwise) and d_lc2 one
+ * device double that receives the LC2 value. All work is enqueued on
+ * `stream` (a cudaStream_t, NULL = default stream); the call returns after
+ * reading back the input maxima, with the result still pending on `stream`.
+ *
+ * No memory is allocated: the resampled image, its Sobel magnitude and the
+ * sums live in one static device array of 256 B + 8 B per voxel for at most
+ * LC2_NOALLOC_MAX_VOXELS virtual voxels (8 MiB), which every GPU that loads
+ * the library holds until the process exits; larger grids are rejected with
+ * LC2_ERR_UNSUPPORTED. The first call on a device looks up that array's
+ * device address (cudaGetSymbolAddress, with the device current), so make
+ * it before any stream capture. Every call shares the array: calls that
+ * overlap on the GPU (other streams, other host threads on the same device)
+ * race and must be serialised by the caller. */
+#define LC2_NOALLOC_MAX_VOXELS (1 << 20)
+int lc2_evaluate_noalloc(int mode, const lc2_geometry* virt, const lc2_geometry* moving,
+                         int patch_size, const float* d_ultrasound, const float* d_moving,
+                         const float* matrix, double* d_lc2, void* stream);
+
 /* Message of the last failure on the calling thread ("" if none). */
 const char* lc2_last_error(void);
 

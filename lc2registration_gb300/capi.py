@@ -35,6 +35,7 @@ EXPORTED = [
     "lc2_get_stream", "lc2_set_stream", "lc2_evaluate_fields", "lc2_launch_count",
     "lc2_enable_kernel_timing", "lc2_kernel_times", "lc2_set_option",
     "lc2_affine_3d", "lc2_affine_2d", "lc2_invert_affine_3d", "lc2_last_error", "lc2_version",
+    "lc2_evaluate_noalloc",
 ]
 
 
@@ -95,6 +96,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "lc2_invert_affine_3d": ([_fp, _fp], ctypes.c_int),
         "lc2_last_error": ([], ctypes.c_char_p),
         "lc2_version": ([], ctypes.c_char_p),
+        "lc2_evaluate_noalloc": ([ctypes.c_int, ctypes.POINTER(lc2_geometry),
+                                  ctypes.POINTER(lc2_geometry), ctypes.c_int, vp, vp, _fp, vp,
+                                  vp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

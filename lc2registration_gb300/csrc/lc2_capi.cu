@@ -50,6 +50,9 @@ size_t elem_size(int storage) { return storage == LC2_STORE_F32 ? 4 : 2; }
 
 }  // namespace
 
+// Message for lc2_last_error from the other translation units.
+void lc2_set_error_message(const char* msg) { g_err = msg ? msg : ""; }
+
 struct lc2_context {
   lc2_config cfg{};
   int warp_nd = 3;  // dimensionality of the resampling
