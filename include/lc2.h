@@ -149,6 +149,76 @@ int lc2_affine_2d(float rotation, const float translation[2], const float scale[
  * LC2_ERR_SINGULAR when the determinant is 0. */
 int lc2_invert_affine_3d(const float in[16], float out[16]);
 
+/* ---- Optimizers (NLopt's role in the reference) ----
+ * Derivative-free, bound-constrained minimisation whose objective receives a
+ * batch of points per call (count x dim, row-major) and writes count values;
+ * a non-zero return aborts with that status. Replaces the NLopt calls of
+ * Optimizers{2D,3D,2DTo3D}::Optimize (src/Optimizers/optimizers.cu:298-302,
+ * 385-390, 854-863, 937-946, 1473-1477, 1548-1553): LC2_OPT_DIRECT_L for
+ * GN_ORIG_DIRECT_L, LC2_OPT_BOBYQA for LN_BOBYQA (a separable quadratic-model
+ * trust region on 2n+1-point stencils; not Powell's update formulas),
+ * LC2_OPT_NELDER_MEAD for LN_NELDERMEAD. xtol_rel is measured in units of
+ * (upper - lower) per entry. */
+typedef int (*lc2_batch_objective)(void* user, int count, int dim, const double* x, double* f);
+enum { LC2_OPT_DIRECT_L = 1, LC2_OPT_BOBYQA = 2, LC2_OPT_NELDER_MEAD = 3 };
+typedef struct {
+    int algorithm;        /* LC2_OPT_* */
+    int dim;
+    const double* lower;  /* dim entries */
+    const double* upper;
+    double xtol_rel;      /* stop when steps fall below xtol_rel * (upper - lower) */
+    int maxeval;          /* 0 = no limit */
+    double initial_step;  /* fraction of (upper - lower); 0 = 0.1 */
+} lc2_opt_problem;
+typedef struct {
+    int evaluations;
+    int batches;          /* objective calls (one batched launch each) */
+} lc2_opt_report;
+/* Minimises f from x (clamped to the bounds); x receives the best point. */
+int lc2_minimize(const lc2_opt_problem* problem, lc2_batch_objective f, void* user, double* x,
+                 double* fmin, lc2_opt_report* report);
+
+/* Registration driver: the DIRECT stage on the entries of direct_entries,
+ * then up to 8 local rounds on their entries, minimising -log(LC2) with
+ * every optimizer step evaluated as one batched launch on `ctx`. Mirrors
+ * Optimizers{2D,3D}::Optimize (src/Optimizers/optimizers.cu:183-410,
+ * 734-970). Parameters follow the reference's order: 2D TX TY R ScaleX
+ * ScaleY Shear (6); 3D and 2D-to-3D TX TY TZ RX RY RZ ScaleX..Z ShearX..Z
+ * (12). Bounds are absolute (the reference adds its translation and
+ * rotation bounds to InitialValues, optimizers.cu:46-57, before this). */
+enum { LC2_ENTRY_TRANSLATION = 1, LC2_ENTRY_ROTATION = 2, LC2_ENTRY_SCALE = 4,
+       LC2_ENTRY_SHEAR = 8 };
+typedef struct {
+    int mode;              /* must match the context */
+    double initial[12];
+    double lower[12];
+    double upper[12];
+    float center[3];       /* rotation centre: the fixed image's centre */
+    float shift[3];        /* moving centre - virtual centre when centred, else 0 */
+    int direct_entries;    /* LC2_ENTRY_* mask; 0 = no DIRECT stage */
+    int direct_maxeval;
+    int rounds;            /* local rounds (<= 8) */
+    int round_entries[8];  /* LC2_ENTRY_* mask per round; 0 = round disabled */
+    double round_xtol[8];  /* the round's AbsTol */
+    int round_maxeval;     /* per round; 0 = no limit */
+    int local_algorithm;   /* LC2_OPT_BOBYQA (default) or LC2_OPT_NELDER_MEAD */
+    /* When lc2_register gets no context: LC2 of `count` matrices (row-major
+     * 3x3 or 4x4 as doubles, dim = 9 or 16) from this callback instead, e.g.
+     * a reference implementation for comparisons. */
+    lc2_batch_objective lc2_of_matrices;
+    void* user;
+} lc2_registration;
+typedef struct {
+    double params[12];     /* optimum, reference order */
+    double lc2;            /* LC2 at the optimum */
+    int evaluations;
+    int launches;          /* batched objective launches */
+} lc2_registration_result;
+int lc2_register(lc2_context* ctx, const lc2_registration* reg, lc2_registration_result* out);
+/* the similarity of one parameter vector as lc2_register sees it */
+int lc2_params_to_matrix(int mode, const double* params, const float center[3],
+                         const float shift[3], float* matrix);
+
 /* Evaluation for callers that cannot allocate device memory: a host
  * application whose allocator or memory pool owns the device heap, a
  * real-time loop that must not allocate after start-up, a plug-in handed

@@ -35,8 +35,42 @@ EXPORTED = [
     "lc2_get_stream", "lc2_set_stream", "lc2_evaluate_fields", "lc2_launch_count",
     "lc2_enable_kernel_timing", "lc2_kernel_times", "lc2_set_option",
     "lc2_affine_3d", "lc2_affine_2d", "lc2_invert_affine_3d", "lc2_last_error", "lc2_version",
-    "lc2_evaluate_noalloc",
+    "lc2_evaluate_noalloc", "lc2_minimize", "lc2_register", "lc2_params_to_matrix",
 ]
+
+ALGORITHMS = {"direct_l": 1, "bobyqa": 2, "nelder_mead": 3}
+ENTRIES = {"translation": 1, "rotation": 2, "scale": 4, "shear": 8}
+
+BATCH_OBJECTIVE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                   ctypes.POINTER(ctypes.c_double),
+                                   ctypes.POINTER(ctypes.c_double))
+
+
+class lc2_opt_problem(ctypes.Structure):
+    _fields_ = [("algorithm", ctypes.c_int), ("dim", ctypes.c_int),
+                ("lower", ctypes.POINTER(ctypes.c_double)),
+                ("upper", ctypes.POINTER(ctypes.c_double)), ("xtol_rel", ctypes.c_double),
+                ("maxeval", ctypes.c_int), ("initial_step", ctypes.c_double)]
+
+
+class lc2_opt_report(ctypes.Structure):
+    _fields_ = [("evaluations", ctypes.c_int), ("batches", ctypes.c_int)]
+
+
+class lc2_registration(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int), ("initial", ctypes.c_double * 12),
+                ("lower", ctypes.c_double * 12), ("upper", ctypes.c_double * 12),
+                ("center", ctypes.c_float * 3), ("shift", ctypes.c_float * 3),
+                ("direct_entries", ctypes.c_int), ("direct_maxeval", ctypes.c_int),
+                ("rounds", ctypes.c_int), ("round_entries", ctypes.c_int * 8),
+                ("round_xtol", ctypes.c_double * 8), ("round_maxeval", ctypes.c_int),
+                ("local_algorithm", ctypes.c_int), ("lc2_of_matrices", BATCH_OBJECTIVE),
+                ("user", ctypes.c_void_p)]
+
+
+class lc2_registration_result(ctypes.Structure):
+    _fields_ = [("params", ctypes.c_double * 12), ("lc2", ctypes.c_double),
+                ("evaluations", ctypes.c_int), ("launches", ctypes.c_int)]
 
 
 class LC2Error(RuntimeError):
@@ -96,6 +130,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "lc2_invert_affine_3d": ([_fp, _fp], ctypes.c_int),
         "lc2_last_error": ([], ctypes.c_char_p),
         "lc2_version": ([], ctypes.c_char_p),
+        "lc2_minimize": ([ctypes.POINTER(lc2_opt_problem), BATCH_OBJECTIVE, vp, _dp, _dp,
+                          ctypes.POINTER(lc2_opt_report)], ctypes.c_int),
+        "lc2_register": ([vp, ctypes.POINTER(lc2_registration),
+                          ctypes.POINTER(lc2_registration_result)], ctypes.c_int),
+        "lc2_params_to_matrix": ([ctypes.c_int, _dp, _fp, _fp, _fp], ctypes.c_int),
         "lc2_evaluate_noalloc": ([ctypes.c_int, ctypes.POINTER(lc2_geometry),
                                   ctypes.POINTER(lc2_geometry), ctypes.c_int, vp, vp, _fp, vp,
                                   vp], ctypes.c_int),
@@ -269,3 +308,112 @@ def invert_affine_3d(mat) -> np.ndarray:
     out = np.zeros(16, dtype=np.float32)
     _check(lib.lc2_invert_affine_3d(m.ctypes.data_as(_fp), out.ctypes.data_as(_fp)))
     return out.reshape(4, 4)
+
+
+def minimize(fun_batch, x0, lower, upper, algorithm: str = "bobyqa", xtol_rel: float = 1e-4,
+             maxeval: int = 0, initial_step: float = 0.0):
+    """Runs lc2_minimize with a Python batch objective fun_batch(X[count, dim]) -> f[count].
+    Returns (x, fmin, evaluations, batches)."""
+    lib = load()
+    n = len(x0)
+    lo = np.ascontiguousarray(lower, dtype=np.float64)
+    hi = np.ascontiguousarray(upper, dtype=np.float64)
+    x = np.ascontiguousarray(x0, dtype=np.float64).copy()
+    err = []
+
+    def cb(user, count, dim, xp, fp):
+        try:
+            X = np.ctypeslib.as_array(xp, shape=(count * dim,)).reshape(count, dim).copy()
+            F = np.asarray(fun_batch(X), dtype=np.float64)
+            np.ctypeslib.as_array(fp, shape=(count,))[:] = F
+            return 0
+        except Exception as e:  # surfaced after the call
+            err.append(e)
+            return 1
+
+    cfun = BATCH_OBJECTIVE(cb)
+    p = lc2_opt_problem(ALGORITHMS[algorithm], n, lo.ctypes.data_as(_dp), hi.ctypes.data_as(_dp),
+                        float(xtol_rel), int(maxeval), float(initial_step))
+    rep = lc2_opt_report()
+    fmin = ctypes.c_double()
+    st = lib.lc2_minimize(ctypes.byref(p), cfun, None, x.ctypes.data_as(_dp), ctypes.byref(fmin),
+                          ctypes.byref(rep))
+    if err:
+        raise err[0]
+    _check(st)
+    return x, fmin.value, rep.evaluations, rep.batches
+
+
+def _mask(entries) -> int:
+    if isinstance(entries, int):
+        return entries
+    m = 0
+    for e in entries:
+        m |= ENTRIES[e]
+    return m
+
+
+def register(ctx, initial, lower, upper, center, shift=(0.0, 0.0, 0.0), direct_entries=(),
+             direct_maxeval: int = 50, rounds=(), round_maxeval: int = 0,
+             local_algorithm: str = "bobyqa", mode: Optional[str] = None, lc2_of_matrices=None):
+    """lc2_register: DIRECT on direct_entries, then local rounds [(entries, xtol), ...].
+
+    ctx: a Context (GPU objective) or None together with lc2_of_matrices, a
+    Python function mapping a (count, 9|16) float64 array of matrices to LC2
+    values (e.g. the FP64 oracle), and mode. Returns dict(params, lc2,
+    evaluations, launches)."""
+    lib = load()
+    mode = mode or ctx.mode
+    reg = lc2_registration()
+    reg.mode = MODES[mode]
+    n = 6 if mode == "2D" else 12
+    for i in range(n):
+        reg.initial[i] = float(initial[i])
+        reg.lower[i] = float(lower[i])
+        reg.upper[i] = float(upper[i])
+    for a in range(min(3, len(center))):
+        reg.center[a] = float(center[a])
+    for a in range(min(3, len(shift))):
+        reg.shift[a] = float(shift[a])
+    reg.direct_entries = _mask(direct_entries)
+    reg.direct_maxeval = int(direct_maxeval)
+    reg.rounds = len(rounds)
+    for r, (entries, xtol) in enumerate(rounds):
+        reg.round_entries[r] = _mask(entries)
+        reg.round_xtol[r] = float(xtol)
+    reg.round_maxeval = int(round_maxeval)
+    reg.local_algorithm = ALGORITHMS[local_algorithm]
+    err = []
+    if lc2_of_matrices is not None:
+        def cb(user, count, dim, xp, fp):
+            try:
+                M = np.ctypeslib.as_array(xp, shape=(count * dim,)).reshape(count, dim).copy()
+                np.ctypeslib.as_array(fp, shape=(count,))[:] = lc2_of_matrices(M)
+                return 0
+            except Exception as e:
+                err.append(e)
+                return 1
+        reg.lc2_of_matrices = BATCH_OBJECTIVE(cb)
+    out = lc2_registration_result()
+    st = lib.lc2_register(ctx.handle if ctx is not None else None, ctypes.byref(reg),
+                          ctypes.byref(out))
+    if err:
+        raise err[0]
+    _check(st)
+    return dict(params=np.array(out.params[:n]), lc2=out.lc2, evaluations=out.evaluations,
+                launches=out.launches)
+
+
+def params_to_matrix(mode: str, params, center, shift=(0.0, 0.0, 0.0)) -> np.ndarray:
+    lib = load()
+    n = 6 if mode == "2D" else 12
+    p = np.zeros(12, dtype=np.float64)
+    p[:n] = params[:n]
+    c = np.zeros(3, dtype=np.float32)
+    c[:len(center)] = center[:3]
+    sh = np.zeros(3, dtype=np.float32)
+    sh[:len(shift)] = shift[:3]
+    m = np.zeros(9 if mode == "2D" else 16, dtype=np.float32)
+    _check(lib.lc2_params_to_matrix(MODES[mode], p.ctypes.data_as(_dp), c.ctypes.data_as(_fp),
+                                    sh.ctypes.data_as(_fp), m.ctypes.data_as(_fp)))
+    return m.reshape(3, 3) if mode == "2D" else m.reshape(4, 4)

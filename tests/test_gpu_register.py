@@ -1,0 +1,57 @@
+"""Registration through lc2_register: the same driver and optimizers run with
+the GPU objective and with the FP64 oracle objective from the same start;
+the recovered parameters must agree within 0.01 mm / 0.01 degree (and 0.01%
+in scale/shear), and both must land near the transform that generated the
+synthetic ultrasound."""
+import numpy as np
+import pytest
+
+from lc2registration_gb300 import capi, synth
+from tests.helpers import make_context, oracle_eval
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(case, init, lo, hi, rounds, direct):
+    c = case.fixed_geom.center()
+    kw = dict(center=c, direct_entries=direct, direct_maxeval=50, rounds=rounds)
+    ctx = make_context(case)
+    gpu = capi.register(ctx, init, lo, hi, **kw)
+    mat_shape = (3, 3) if case.mode == "2D" else (4, 4)
+    orc = capi.register(None, init, lo, hi, mode=case.mode,
+                        lc2_of_matrices=lambda M: np.array(
+                            [oracle_eval(case, m.reshape(mat_shape)) for m in M]), **kw)
+    return gpu, orc
+
+
+def test_register_2d_gpu_matches_oracle_and_truth():
+    case = synth.case_2d(seed=1, size=128, r=3)
+    p = case.true_params
+    true = np.array(list(p["trans"]) + [p["rot"]] + list(p["scale"]) + [p["shear"]])
+    init = np.array([0, 0, 0, 1, 1, 0.0])
+    lo = np.array([-10, -10, -8, 0.9, 0.9, -0.06])
+    hi = np.array([10, 10, 8, 1.1, 1.1, 0.06])
+    rounds = [(["translation", "rotation"], 1e-4),
+              (["translation", "rotation", "scale", "shear"], 1e-4)]
+    gpu, orc = _run(case, init, lo, hi, rounds, ["translation"])
+    d = np.abs(gpu["params"] - orc["params"])
+    assert d[:3].max() <= 0.01, d            # mm, mm, degree
+    assert d[3:].max() <= 1e-4, d            # scale, shear
+    assert abs(gpu["lc2"] / orc["lc2"] - 1) < 1e-5
+    assert np.abs(gpu["params"][:2] - true[:2]).max() < 0.5
+    assert abs(gpu["params"][2] - true[2]) < 0.5
+    assert gpu["launches"] < gpu["evaluations"] / 3
+
+
+def test_register_3d_gpu_matches_oracle():
+    case = synth.case_3d(seed=5, mr_size=40, us_size=32, r=2, blobs=6)
+    p = case.true_params
+    init = np.array([0, 0, 0, 0, 0, 0, 1, 1, 1, 0, 0, 0.0])
+    lo = np.array([-10, -10, -10, -8, -8, -8, 0.9, 0.9, 0.9, -0.05, -0.05, -0.05])
+    hi = -lo.copy()
+    hi[6:9] = 1.1
+    rounds = [(["translation", "rotation"], 1e-3)]
+    gpu, orc = _run(case, init, lo, hi, rounds, ["translation"])
+    d = np.abs(gpu["params"] - orc["params"])
+    assert d[:6].max() <= 0.01, d
+    assert np.abs(gpu["params"][:3] - np.array(p["trans"])).max() < 1.5
