@@ -207,6 +207,15 @@ typedef struct {
      * a reference implementation for comparisons. */
     lc2_batch_objective lc2_of_matrices;
     void* user;
+    /* Optional: called after every batch with the stage (0 = DIRECT, r + 1 =
+     * local round r, rounds + 1 = the final evaluation at the optimum), the
+     * `count` parameter vectors (reference order, 6 or 12 entries each) and
+     * their LC2 values, e.g. to write RegistrationInfo.log
+     * (src/Optimizers/optimizers.cu:709-720). Every evaluation counted in
+     * lc2_registration_result.evaluations is reported exactly once. */
+    void (*observer)(void* user, int stage, int count, int nparams, const double* params,
+                     const double* lc2);
+    void* observer_user;
 } lc2_registration;
 typedef struct {
     double params[12];     /* optimum, reference order */

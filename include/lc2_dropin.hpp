@@ -35,6 +35,15 @@
 #include <vector>
 
 #include "lc2.h"
+#include "lc2_yaml.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cstdint>
+#include <cstring>
+#include <ctime>
+#include <fstream>
+#include <sstream>
 
 #ifndef LC2PARAMETERS
 #define LC2PARAMETERS
@@ -115,6 +124,119 @@ class Context {
   lc2_context* ctx_ = nullptr;
 };
 
+// ------------------------------------------------------------ volume I/O
+// A float32 image/volume with its geometry (2D images: dim[2] = 1).
+struct Volume {
+  std::vector<float> data;
+  int dim[3] = {1, 1, 1};
+  float spacing[3] = {1.0f, 1.0f, 1.0f};
+  float origin[3] = {0.0f, 0.0f, 0.0f};
+};
+
+// Raw float32, x fastest (readFromBin, src/Utilities/my_cuda_helper.cu:25-42).
+inline std::vector<float> read_raw_floats(const std::string& path, size_t n) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw Error(LC2_ERR_INVALID_ARGUMENT, "cannot open " + path);
+  std::vector<float> v(n);
+  f.read(reinterpret_cast<char*>(v.data()), (std::streamsize)(sizeof(float) * n));
+  if (!f) throw Error(LC2_ERR_INVALID_ARGUMENT, "short read: " + path);
+  return v;
+}
+
+// Minimal NRRD reader: raw encoding, little endian, scalar types, sizes,
+// spacings or diagonal space directions, space origin, inline or detached
+// data. (The reference reads NRRD through ITK, volumeImporter.cpp:42-93.)
+inline Volume read_nrrd(const std::string& path) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw Error(LC2_ERR_INVALID_ARGUMENT, "cannot open " + path);
+  std::string line;
+  std::getline(f, line);
+  if (line.rfind("NRRD", 0) != 0) throw Error(LC2_ERR_INVALID_ARGUMENT, path + ": not NRRD");
+  std::string type = "float", encoding = "raw", endian = "little", datafile;
+  int ndim = 0;
+  Volume v;
+  auto vec3 = [](const std::string& s, float* out, int n) {
+    std::string t = s;
+    for (char& c : t)
+      if (c == '(' || c == ')' || c == ',') c = ' ';
+    std::istringstream in(t);
+    for (int i = 0; i < n; ++i) in >> out[i];
+  };
+  while (std::getline(f, line)) {
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    if (line.empty()) break;
+    if (line[0] == '#') continue;
+    const size_t c = line.find(':');
+    if (c == std::string::npos) continue;
+    std::string key = line.substr(0, c), val = line.substr(c + 1);
+    if (!val.empty() && val[0] == '=') val = val.substr(1);
+    while (!val.empty() && val[0] == ' ') val.erase(0, 1);
+    if (key == "type") type = val;
+    else if (key == "dimension") ndim = std::atoi(val.c_str());
+    else if (key == "sizes") {
+      std::istringstream in(val);
+      for (int i = 0; i < ndim && i < 3; ++i) in >> v.dim[i];
+    } else if (key == "spacings") {
+      std::istringstream in(val);
+      for (int i = 0; i < ndim && i < 3; ++i) in >> v.spacing[i];
+    } else if (key == "space directions") {
+      float d[9] = {0};
+      vec3(val, d, ndim * ndim);
+      for (int i = 0; i < ndim && i < 3; ++i) v.spacing[i] = std::fabs(d[i * ndim + i]);
+    } else if (key == "space origin") {
+      vec3(val, v.origin, ndim);
+    } else if (key == "encoding") encoding = val;
+    else if (key == "endian") endian = val;
+    else if (key == "data file" || key == "datafile") datafile = val;
+  }
+  if (encoding != "raw" || endian != "little")
+    throw Error(LC2_ERR_UNSUPPORTED, path + ": only raw little-endian NRRD is supported");
+  const size_t n = (size_t)v.dim[0] * v.dim[1] * v.dim[2];
+  std::ifstream df;
+  std::istream* in = &f;
+  if (!datafile.empty()) {
+    std::string dir = path.substr(0, path.find_last_of('/') + 1);
+    df.open(datafile[0] == '/' ? datafile : dir + datafile, std::ios::binary);
+    in = &df;
+  }
+  v.data.resize(n);
+  auto rd = [&](auto tag) {
+    using T = decltype(tag);
+    std::vector<T> tmp(n);
+    in->read(reinterpret_cast<char*>(tmp.data()), (std::streamsize)(sizeof(T) * n));
+    if (!*in) throw Error(LC2_ERR_INVALID_ARGUMENT, path + ": short read");
+    for (size_t i = 0; i < n; ++i) v.data[i] = (float)tmp[i];
+  };
+  if (type == "float") rd(float());
+  else if (type == "double") rd(double());
+  else if (type == "short" || type == "int16") rd(int16_t());
+  else if (type == "ushort" || type == "unsigned short" || type == "uint16") rd(uint16_t());
+  else if (type == "int" || type == "int32") rd(int32_t());
+  else if (type == "uchar" || type == "unsigned char" || type == "uint8") rd(uint8_t());
+  else throw Error(LC2_ERR_UNSUPPORTED, path + ": NRRD type " + type);
+  return v;
+}
+
+// Volume from a FixedVolume / MovingVolume / FixedImage / MovingImage node:
+// FilePath with Format raw (Dimension, Spacing, Origin given) or a .nrrd file
+// (geometry from its header, overridden by the node where given).
+inline Volume load_volume(const lc2yaml::Node& d, int nd) {
+  const std::string path = d["FilePath"].str();
+  Volume v;
+  const bool nrrd = path.size() > 5 && path.substr(path.size() - 5) == ".nrrd";
+  if (!nrrd && !d["Dimension"])
+    throw Error(LC2_ERR_UNSUPPORTED, path + ": only raw (with Dimension) and .nrrd are supported");
+  if (nrrd) v = read_nrrd(path);
+  static const char* ax[3] = {"x", "y", "z"};
+  for (int a = 0; a < nd; ++a) {
+    if (d["Dimension"][ax[a]]) v.dim[a] = d["Dimension"][ax[a]].integer();
+    if (d["Spacing"][ax[a]]) v.spacing[a] = (float)d["Spacing"][ax[a]].num();
+    if (d["Origin"][ax[a]]) v.origin[a] = (float)d["Origin"][ax[a]].num();
+  }
+  if (!nrrd) v.data = read_raw_floats(path, (size_t)v.dim[0] * v.dim[1] * v.dim[2]);
+  return v;
+}
+
 // Shared machinery of the three interpolators: geometry, mapper centre and
 // shift (Interpolator3D::InitiateMappers, interpolator.cu:495-529), the
 // current virtual->moving matrix and the evaluation calls.
@@ -146,6 +268,17 @@ class InterpolatorBase {
   bool centered_ = true;
   std::vector<float> matrix_;
   Context ctx_;
+  Volume fixed_vol_, moving_vol_;  // owned images (parameter-file constructors)
+  std::string output_path_;
+
+ public:
+  // Mapper centre and shift of InitiateMappers (for the registration driver).
+  const float* Center() const { return center_; }
+  const float* Shift() const { return shift_; }
+  int Mode() const { return cfg_.mode; }
+  int PatchSize() const { return cfg_.patch_size; }
+
+ protected:
 
   static float geom_center(const lc2_geometry& g, int a) {
     return g.origin[a] + g.spacing[a] * (float)g.dim[a] / 2.0f;
@@ -220,6 +353,42 @@ class Interpolator3D : public InterpolatorBase {
     matrix_.assign({1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1});
   }
 
+  // From a parameter file (Interpolator3D(yaml, useIGTL), interpolator.cu:234-391;
+  // Interpolator2DTo3D(yaml), :1538-1623). The pose side channel is not part of
+  // this path; useIGTL is accepted and ignored.
+  explicit Interpolator3D(const std::string& yaml_path, bool useIGTL = false,
+                          int mode = LC2_MODE_3D) {
+    (void)useIGTL;
+    const lc2yaml::Node y = lc2yaml::load_file(yaml_path);
+    const lc2yaml::Node& in = y["InputParameters"];
+    const lc2yaml::Node& rp = in["RegistrationParameters"];
+    fixed_vol_ = load_volume(in["FixedVolume"], 3);
+    moving_vol_ = load_volume(in["MovingVolume"], 3);
+    cfg_.mode = mode;
+    for (int a = 0; a < 3; ++a) {
+      cfg_.fixed.dim[a] = fixed_vol_.dim[a];
+      cfg_.fixed.spacing[a] = fixed_vol_.spacing[a];
+      cfg_.fixed.origin[a] = fixed_vol_.origin[a];
+      cfg_.moving.dim[a] = moving_vol_.dim[a];
+      cfg_.moving.spacing[a] = moving_vol_.spacing[a];
+      cfg_.moving.origin[a] = moving_vol_.origin[a];
+    }
+    static const char* ax[3] = {"x", "y", "z"};
+    for (int a = 0; a < 3; ++a)
+      cfg_.virtual_spacing[a] = (float)rp["ResampledSpacing"][ax[a]].num();
+    cfg_.patch_size = rp["PatchSize"].integer();
+    cfg_.high_res_is_moving = rp["HighResolutionModality"].str() == "Moving" ? 1 : 0;
+    cfg_.storage = LC2_STORE_F32;
+    centered_ = rp["CenterOverlaid"].boolean();
+    if (rp["FinalRoundExportRootPath"]) output_path_ = rp["FinalRoundExportRootPath"].str();
+    fixed_ = fixed_vol_.data.data();
+    moving_ = moving_vol_.data.data();
+    configured_ = true;
+    matrix_.assign({1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1});
+  }
+
+  std::string GetOutputPath() { return output_path_; }
+
   void InitiateMappers() { mappers(3); }
   void InitiateRegistrationHandle() { handle(); }
 
@@ -260,6 +429,8 @@ class Interpolator2DTo3D : public Interpolator3D {
  public:
   explicit Interpolator2DTo3D(const LC2Configuration2DTo3D* c)
       : Interpolator3D(c, LC2_MODE_2DTO3D) {}
+  explicit Interpolator2DTo3D(const std::string& yaml_path)
+      : Interpolator3D(yaml_path, false, LC2_MODE_2DTO3D) {}
 };
 
 // 2D registration.
@@ -289,6 +460,40 @@ class Interpolator2D : public InterpolatorBase {
     configured_ = true;
     matrix_.assign({1, 0, 0, 0, 1, 0, 0, 0, 1});
   }
+
+  // From a parameter file (Interpolator2D(yaml), interpolator.cu:979-1103).
+  explicit Interpolator2D(const std::string& yaml_path) {
+    const lc2yaml::Node y = lc2yaml::load_file(yaml_path);
+    const lc2yaml::Node& in = y["InputParameters"];
+    const lc2yaml::Node& rp = in["RegistrationParameters"];
+    fixed_vol_ = load_volume(in["FixedImage"], 2);
+    moving_vol_ = load_volume(in["MovingImage"], 2);
+    cfg_.mode = LC2_MODE_2D;
+    for (int a = 0; a < 2; ++a) {
+      cfg_.fixed.dim[a] = fixed_vol_.dim[a];
+      cfg_.fixed.spacing[a] = fixed_vol_.spacing[a];
+      cfg_.fixed.origin[a] = fixed_vol_.origin[a];
+      cfg_.moving.dim[a] = moving_vol_.dim[a];
+      cfg_.moving.spacing[a] = moving_vol_.spacing[a];
+      cfg_.moving.origin[a] = moving_vol_.origin[a];
+    }
+    cfg_.fixed.dim[2] = cfg_.moving.dim[2] = 1;
+    cfg_.fixed.spacing[2] = cfg_.moving.spacing[2] = 1.0f;
+    cfg_.virtual_spacing[0] = (float)rp["ResampledSpacing"]["x"].num();
+    cfg_.virtual_spacing[1] = (float)rp["ResampledSpacing"]["y"].num();
+    cfg_.virtual_spacing[2] = 1.0f;
+    cfg_.patch_size = rp["PatchSize"].integer();
+    cfg_.high_res_is_moving = rp["HighResolutionModality"].str() == "Moving" ? 1 : 0;
+    cfg_.storage = LC2_STORE_F32;
+    centered_ = rp["CenterOverlaid"].boolean();
+    if (rp["FinalRoundExportRootPath"]) output_path_ = rp["FinalRoundExportRootPath"].str();
+    fixed_ = fixed_vol_.data.data();
+    moving_ = moving_vol_.data.data();
+    configured_ = true;
+    matrix_.assign({1, 0, 0, 0, 1, 0, 0, 0, 1});
+  }
+
+  std::string GetOutputPath() { return output_path_; }
 
   void InitiateMappers() { mappers(2); }
   void InitiateRegistrationHandle() { handle(); }

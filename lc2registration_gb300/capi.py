@@ -41,6 +41,8 @@ EXPORTED = [
 ALGORITHMS = {"direct_l": 1, "bobyqa": 2, "nelder_mead": 3}
 ENTRIES = {"translation": 1, "rotation": 2, "scale": 4, "shear": 8}
 
+OBSERVER = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double))
 BATCH_OBJECTIVE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                    ctypes.POINTER(ctypes.c_double),
                                    ctypes.POINTER(ctypes.c_double))
@@ -65,7 +67,8 @@ class lc2_registration(ctypes.Structure):
                 ("rounds", ctypes.c_int), ("round_entries", ctypes.c_int * 8),
                 ("round_xtol", ctypes.c_double * 8), ("round_maxeval", ctypes.c_int),
                 ("local_algorithm", ctypes.c_int), ("lc2_of_matrices", BATCH_OBJECTIVE),
-                ("user", ctypes.c_void_p)]
+                ("user", ctypes.c_void_p), ("observer", ctypes.c_void_p),
+                ("observer_user", ctypes.c_void_p)]
 
 
 class lc2_registration_result(ctypes.Structure):
@@ -355,12 +358,14 @@ def _mask(entries) -> int:
 
 def register(ctx, initial, lower, upper, center, shift=(0.0, 0.0, 0.0), direct_entries=(),
              direct_maxeval: int = 50, rounds=(), round_maxeval: int = 0,
-             local_algorithm: str = "bobyqa", mode: Optional[str] = None, lc2_of_matrices=None):
+             local_algorithm: str = "bobyqa", mode: Optional[str] = None, lc2_of_matrices=None,
+             observer=None):
     """lc2_register: DIRECT on direct_entries, then local rounds [(entries, xtol), ...].
 
     ctx: a Context (GPU objective) or None together with lc2_of_matrices, a
     Python function mapping a (count, 9|16) float64 array of matrices to LC2
-    values (e.g. the FP64 oracle), and mode. Returns dict(params, lc2,
+    values (e.g. the FP64 oracle), and mode. observer(stage, params (count, n),
+    lc2 (count,)) sees every evaluation. Returns dict(params, lc2,
     evaluations, launches)."""
     lib = load()
     mode = mode or ctx.mode
@@ -394,6 +399,15 @@ def register(ctx, initial, lower, upper, center, shift=(0.0, 0.0, 0.0), direct_e
                 err.append(e)
                 return 1
         reg.lc2_of_matrices = BATCH_OBJECTIVE(cb)
+    if observer is not None:
+        def ob(user, stage, count, nparams, pp, lp):
+            try:
+                P = np.ctypeslib.as_array(pp, shape=(count * nparams,)).reshape(count, nparams)
+                observer(stage, P.copy(), np.ctypeslib.as_array(lp, shape=(count,)).copy())
+            except Exception as e:  # an observer cannot fail the C driver
+                err.append(e)
+        ob_c = OBSERVER(ob)
+        reg.observer = ctypes.cast(ob_c, ctypes.c_void_p)
     out = lc2_registration_result()
     st = lib.lc2_register(ctx.handle if ctx is not None else None, ctypes.byref(reg),
                           ctypes.byref(out))

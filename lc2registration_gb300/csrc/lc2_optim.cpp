@@ -395,6 +395,7 @@ struct RegObjective {
   std::vector<float> mats;
   std::vector<double> lc2;
   long long evaluations = 0;
+  int stage = 0;  // 0 = DIRECT, r + 1 = local round r
 };
 
 int params_of(int mode) { return mode == LC2_MODE_2D ? 6 : 12; }
@@ -453,6 +454,15 @@ int reg_objective(void* user, int count, int dim, const double* x, double* f) {
     const double v = o->lc2[k];
     f[k] = (v > 0.0) ? -std::log(v) : std::numeric_limits<double>::max();
   }
+  if (o->reg->observer) {
+    const int np = params_of(mode);
+    std::vector<double> all((size_t)count * np);
+    for (int k = 0; k < count; ++k) {
+      for (int j = 0; j < np; ++j) all[(size_t)k * np + j] = o->base[j];
+      for (int j = 0; j < dim; ++j) all[(size_t)k * np + o->map[j]] = x[(size_t)k * dim + j];
+    }
+    o->reg->observer(o->reg->observer_user, o->stage, count, np, all.data(), o->lc2.data());
+  }
   o->evaluations += count;
   return 0;
 }
@@ -503,13 +513,17 @@ extern "C" int lc2_register(lc2_context* ctx, const lc2_registration* reg,
     return LC2_OK;
   };
   int st = LC2_OK;
-  if (reg->direct_entries)
+  if (reg->direct_entries) {
+    o.stage = 0;
     st = stage(LC2_OPT_DIRECT_L, reg->direct_entries, 1e-4, reg->direct_maxeval);
+  }
   const int local = reg->local_algorithm ? reg->local_algorithm : LC2_OPT_BOBYQA;
   for (int r = 0; st == LC2_OK && r < reg->rounds; ++r)
-    if (reg->round_entries[r])
+    if (reg->round_entries[r]) {
+      o.stage = r + 1;
       st = stage(local, reg->round_entries[r], reg->round_xtol[r] > 0 ? reg->round_xtol[r] : 1e-4,
                  reg->round_maxeval);
+    }
   if (st != LC2_OK) return st;
   // similarity at the optimum
   const int mf = (reg->mode == LC2_MODE_2D) ? 9 : 16;
@@ -524,6 +538,8 @@ extern "C" int lc2_register(lc2_context* ctx, const lc2_registration* reg,
     }
   }
   if (st != LC2_OK) return st;
+  if (reg->observer)
+    reg->observer(reg->observer_user, reg->rounds + 1, 1, np, o.base.data(), &out->lc2);
   for (int i = 0; i < 12; ++i) out->params[i] = (i < np) ? o.base[i] : 0.0;
   out->evaluations = (int)o.evaluations + 1;
   out->launches = launches + 1;

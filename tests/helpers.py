@@ -62,3 +62,78 @@ def perturbed(case: Case, rng, n: int, scale: float = 1.0):
                                 [s + scale * rng.uniform(-0.02, 0.02) for s in p["shear"]], c,
                                 (0, 0, 0)))
     return np.stack(out)
+
+
+def write_param_file(tmp_path, case, name="params.yaml", direct=True, rounds=None,
+                     centred=False, patch=None):
+    """Writes a parameter file in the reference's schema (config/*.yaml) for a
+    synthetic case, with the images as raw float32 files next to it."""
+    nd = 2 if case.mode == "2D" else 3
+    f, m = tmp_path / "fixed.raw", tmp_path / "moving.raw"
+    case.fixed.astype(np.float32).tofile(f)
+    case.moving.astype(np.float32).tofile(m)
+    ax = ["x", "y", "z"][:nd]
+
+    def geo(g):
+        d = ", ".join(f"{a}: {int(g.dim[i])}" for i, a in enumerate(ax))
+        s = ", ".join(f"{a}: {g.spacing[i]!r}" for i, a in enumerate(ax))
+        o = ", ".join(f"{a}: {g.origin[i]!r}" for i, a in enumerate(ax))
+        return f"{{{d}}}", f"{{{s}}}", f"{{{o}}}"
+
+    fd, fs, fo = geo(case.fixed_geom)
+    md, ms, mo = geo(case.moving_geom)
+    img = "Image" if nd == 2 else "Volume"
+    vs = ", ".join(f"{a}: {case.virt_spacing[i]!r}" for i, a in enumerate(ax))
+    if nd == 2:
+        keys = ["TX", "TY", "R", "ScaleX", "ScaleY", "Shear"]
+        init = [0, 0, 0, 1, 1, 0]
+        lo = [-10, -10, -8, 0.9, 0.9, -0.06]
+        hi = [10, 10, 8, 1.1, 1.1, 0.06]
+    else:
+        keys = ["TX", "TY", "TZ", "RX", "RY", "RZ", "ScaleX", "ScaleY", "ScaleZ", "ShearX",
+                "ShearY", "ShearZ"]
+        init = [0, 0, 0, 0, 0, 0, 1, 1, 1, 0, 0, 0]
+        lo = [-10, -10, -10, -8, -8, -8, 0.9, 0.9, 0.9, -0.05, -0.05, -0.05]
+        hi = [10, 10, 10, 8, 8, 8, 1.1, 1.1, 1.1, 0.05, 0.05, 0.05]
+    kv = lambda vals: "{" + ", ".join(f"{k}: {float(v)!r}" for k, v in zip(keys, vals)) + "}"
+    rounds = rounds or [("true", "true", "false", "false", "1.0e-4"),
+                        ("true", "true", "true", "true", "1.0e-4")]
+    lines = [
+        "InputParameters:",
+        f"  Fixed{img}:",
+        f"    Dimension: {fd}",
+        f"    Spacing: {fs}",
+        f"    Origin: {fo}",
+        f"    FilePath: {f}",
+        "    Format: raw",
+        "    DataType: float32",
+        f"  Moving{img}:",
+        f"    Dimension: {md}",
+        f"    Spacing: {ms}",
+        f"    Origin: {mo}",
+        f"    FilePath: {m}  # raw float32",
+        "    Format: raw",
+        "  RegistrationParameters:",
+        f"    HighResolutionModality: {'Moving' if case.hr_moving else 'Fixed'}",
+        "    Type: Affine",
+        f"    ResampledSpacing: {{{vs}}}",
+        f"    PatchSize: {patch or case.r}",
+        f"    FinalRoundExportRootPath: {tmp_path}",
+        f"    CenterOverlaid: {'true' if centred else 'false'}",
+        "  OptimizerSettings:",
+        f"    InitialValues: {kv(init)}",
+        f"    LowerBounds: {kv([l - i if k in ('TX', 'TY', 'TZ', 'R', 'RX', 'RY', 'RZ') else l for k, l, i in zip(keys, lo, init)])}",
+        f"    UpperBounds: {kv([h - i if k in ('TX', 'TY', 'TZ', 'R', 'RX', 'RY', 'RZ') else h for k, h, i in zip(keys, hi, init)])}",
+        "    DIRECT:",
+        f"      Enabled: {'true' if direct else 'false'}",
+        "      OptimizedEntries: {Translation: true, Rotation: false, Scale: false, Shear: false}",
+        "      MaxEvaluations: 50",
+        "    BOBYQA:",
+    ]
+    for r, (t, ro, s, sh, tol) in enumerate(rounds):
+        lines += [f"      {r}:", "        Enabled: true",
+                  f"        OptimizedEntries: {{Translation: {t}, Rotation: {ro}, Scale: {s}, Shear: {sh}}}",
+                  f"        AbsTol: {tol}"]
+    p = tmp_path / name
+    p.write_text("\n".join(lines) + "\n")
+    return p

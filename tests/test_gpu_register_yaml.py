@@ -1,0 +1,87 @@
+"""The reference's registration flow from a parameter file
+(Interpolator(yaml) -> Optimizers(yaml) -> Optimize -> ExportResults) through
+the C++ drop-in headers, against lc2_register called directly with the same
+settings, and the files it writes (RegistrationInfo.log, <name>_result.yaml)."""
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from lc2registration_gb300 import capi, synth
+from tests.helpers import make_context, write_param_file
+from tests.test_yaml import build_register
+
+pytestmark = pytest.mark.gpu
+
+ROUNDS = [("true", "true", "false", "false", "1.0e-4"),
+          ("true", "true", "true", "true", "1.0e-4")]
+
+
+def _flow(text, key):
+    m = re.search(rf"^\s*{key}: \{{(.*)\}}$", text, re.M)
+    return {k.strip(): float(v) for k, v in (kv.split(":") for kv in m.group(1).split(","))}
+
+
+def _run(tmp_path, mode, case, lo, hi):
+    exe = build_register(tmp_path)
+    p = write_param_file(tmp_path, case, rounds=ROUNDS)
+    out = subprocess.run([exe, mode, str(p)], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    line1, line2 = out.stdout.strip().splitlines()
+    params = np.array([float(v) for v in line1.split()])
+    sim, evals, result = line2.split()
+    init = np.array([0, 0, 0, 1, 1, 0.0]) if mode == "2D" else \
+        np.array([0, 0, 0, 0, 0, 0, 1, 1, 1, 0, 0, 0.0])
+    rounds = [(["translation", "rotation"], 1e-4),
+              (["translation", "rotation", "scale", "shear"], 1e-4)]
+    ref = capi.register(make_context(case), init, lo, hi, center=case.fixed_geom.center(),
+                        direct_entries=["translation"], direct_maxeval=50, rounds=rounds)
+    return params, float(sim), int(evals), result, ref
+
+
+def _check_files(tmp_path, result, params, sim, evals, keys, mode, case):
+    text = open(result).read()
+    iv = _flow(text, "InitialValues")
+    got = np.array([iv[k] for k in keys])
+    np.testing.assert_allclose(got, params.astype(np.float32), rtol=1e-6, atol=1e-7)
+    assert re.search(r"^\s*IsRegistered: true$", text, re.M)
+    assert int(re.search(r"NumEvaluations: (\d+)", text).group(1)) == evals
+    assert abs(float(re.search(r"LastSimilarity: (\S+)", text).group(1)) - sim) < 1e-7
+    d = 3 if mode == "2D" else 4
+    rows = re.findall(r"^\s*-\n((?:\s*- \S+\n){%d})" % d, text, re.M)
+    tm = np.array([[float(v) for v in re.findall(r"- (\S+)", r)] for r in rows[-d:]])
+    m = capi.params_to_matrix(mode, params, case.fixed_geom.center(), (0, 0, 0))
+    np.testing.assert_allclose(tm @ m, np.eye(d), atol=2e-5)
+    log = open(tmp_path / "RegistrationInfo.log").read().strip().splitlines()
+    assert log[0].startswith("Step,Transform[16]")
+    assert len(log) == 1 + 1 + evals        # header, initial row, one row per evaluation
+    assert "Enabled: false" in text          # DIRECT and round 0 disabled for a re-run
+
+
+def test_register_yaml_2d(tmp_path):
+    case = synth.case_2d(seed=1, size=128, r=3)
+    lo = np.array([-10, -10, -8, 0.9, 0.9, -0.06])
+    hi = np.array([10, 10, 8, 1.1, 1.1, 0.06])
+    params, sim, evals, result, ref = _run(tmp_path, "2D", case, lo, hi)
+    np.testing.assert_allclose(params, ref["params"], rtol=1e-7, atol=1e-7)
+    assert abs(sim / ref["lc2"] - 1) < 1e-7 and evals == ref["evaluations"]
+    p = case.true_params
+    assert np.abs(params[:2] - np.array(p["trans"])).max() < 0.5
+    _check_files(tmp_path, result, params, sim, evals,
+                 ["TX", "TY", "R", "ScaleX", "ScaleY", "Shear"], "2D", case)
+
+
+def test_register_yaml_3d(tmp_path):
+    case = synth.case_3d(seed=5, mr_size=40, us_size=32, r=2, blobs=6)
+    lo = np.array([-10, -10, -10, -8, -8, -8, 0.9, 0.9, 0.9, -0.05, -0.05, -0.05])
+    hi = -lo.copy()
+    hi[6:9] = 1.1
+    params, sim, evals, result, ref = _run(tmp_path, "3D", case, lo, hi)
+    np.testing.assert_allclose(params, ref["params"], rtol=1e-7, atol=1e-7)
+    assert abs(sim / ref["lc2"] - 1) < 1e-7 and evals == ref["evaluations"]
+    p = case.true_params
+    assert np.abs(params[:3] - np.array(p["trans"])).max() < 1.5
+    _check_files(tmp_path, result, params, sim, evals,
+                 ["TX", "TY", "TZ", "RX", "RY", "RZ", "ScaleX", "ScaleY", "ScaleZ", "ShearX",
+                  "ShearY", "ShearZ"], "3D", case)

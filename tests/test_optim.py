@@ -55,3 +55,27 @@ def test_maxeval_is_respected_and_errors_propagate():
         capi.minimize(bad, [0.0], [-1.0], [1.0], "nelder_mead")
     with pytest.raises(capi.LC2Error):
         capi.minimize(f, [0.0], [1.0], [-1.0], "bobyqa")
+
+
+def test_register_observer_sees_every_evaluation():
+    """lc2_register with a CPU objective of the matrices: the observer gets
+    each evaluation once, the last one being the optimum (stage rounds + 1)."""
+    center = (8.0, 8.0)
+    target = capi.params_to_matrix("2D", [1.5, -2.0, 3.0, 1.02, 0.98, 0.0], center)
+
+    def lc2(M):
+        d = M.reshape(-1, 9)[:, :6] - target.reshape(9)[:6]
+        return np.exp(-(d * np.array([30, 30, 0.3, 30, 30, 0.3])) ** 2 @ np.ones(6) * 0.1)
+
+    seen = []
+    rounds = [(["translation", "rotation"], 1e-5), (["translation", "rotation", "scale"], 1e-5)]
+    res = capi.register(None, [0, 0, 0, 1, 1, 0], [-5, -5, -8, 0.9, 0.9, -0.05],
+                        [5, 5, 8, 1.1, 1.1, 0.05], center, direct_entries=["translation"],
+                        direct_maxeval=40, rounds=rounds, mode="2D", lc2_of_matrices=lc2,
+                        observer=lambda st, P, L: seen.append((st, P, L)))
+    assert sum(len(L) for _, _, L in seen) == res["evaluations"]
+    stages = [st for st, _, _ in seen]
+    assert stages == sorted(stages) and stages[0] == 0 and stages[-1] == len(rounds) + 1
+    assert len(seen[-1][2]) == 1 and seen[-1][2][0] == res["lc2"]
+    np.testing.assert_array_equal(seen[-1][1][0], res["params"])
+    assert np.abs(res["params"][:3] - [1.5, -2.0, 3.0]).max() < 0.05
