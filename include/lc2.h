@@ -228,6 +228,47 @@ int lc2_register(lc2_context* ctx, const lc2_registration* reg, lc2_registration
 int lc2_params_to_matrix(int mode, const double* params, const float center[3],
                          const float shift[3], float* matrix);
 
+/* ---- 2D-to-3D frame stacks ----
+ * One MR/CT volume against many ultrasound frames of their own sizes and
+ * geometries, with any number of candidate poses per frame, evaluated in one
+ * persistent launch (replayed from a CUDA graph when the frame layout of a
+ * call repeats). Each frame behaves exactly as an LC2_MODE_2DTO3D context
+ * with HighResolutionModality: Moving (Interpolator2DTo3D,
+ * src/Interpolator/interpolator.cu:1538-1775; LC2_2D_class on the frame,
+ * src/cu_LC2/cu_lc2_2d.cu:515-653) that shares the stack's volume: a stack
+ * evaluation returns the same value, bit for bit, as lc2_evaluate on a
+ * standalone context of that frame. The reference evaluates one frame and
+ * one pose per call. */
+typedef struct lc2_stack lc2_stack;
+
+/* Creates an empty stack for a moving volume of geometry `moving`, patch
+ * radius `patch_size` (1..12), storage type (lc2_storage) on `device`. */
+int lc2_stack_create(const lc2_geometry* moving, int patch_size, int storage, int device,
+                     lc2_stack** out);
+/* Releases the stack, its frames and their device memory. */
+int lc2_stack_destroy(lc2_stack* s);
+/* Uploads the moving volume (host float32). Once per stack, before frames. */
+int lc2_stack_set_moving(lc2_stack* s, const float* moving);
+/* Adds a frame: its geometry (dim[2] = 1), virtual spacing and ultrasound
+ * image (host float32); returns its id (0, 1, ...) in *frame_id. */
+int lc2_stack_add_frame(lc2_stack* s, const lc2_geometry* frame, const float virtual_spacing[3],
+                        const float* ultrasound, int* frame_id);
+/* Number of frames. */
+int lc2_stack_frames(const lc2_stack* s);
+/* The frame's own context (owned by the stack; do not destroy or call
+ * lc2_set_images on it), e.g. for lc2_evaluate or lc2_register on one frame. */
+int lc2_stack_frame_context(lc2_stack* s, int frame_id, lc2_context** ctx);
+/* `count` evaluations: frame_ids[k] with the 4x4 virtual->moving matrix
+ * matrices[16 k ..]; lc2[k] receives the LC2 value. Frames may repeat and
+ * come in any order. */
+int lc2_stack_evaluate(lc2_stack* s, int count, const int* frame_ids, const float* matrices,
+                       double* lc2);
+/* CUDA-graph replay of repeated layouts: on (1, default) or off (0). */
+int lc2_stack_set_graphs(lc2_stack* s, int on);
+/* Kernel launches and graph launches issued by the stack since creation. */
+long long lc2_stack_launch_count(const lc2_stack* s);
+long long lc2_stack_graph_launches(const lc2_stack* s);
+
 /* Evaluation for callers that cannot allocate device memory: a host
  * application whose allocator or memory pool owns the device heap, a
  * real-time loop that must not allocate after start-up, a plug-in handed

@@ -36,6 +36,9 @@ EXPORTED = [
     "lc2_enable_kernel_timing", "lc2_kernel_times", "lc2_set_option",
     "lc2_affine_3d", "lc2_affine_2d", "lc2_invert_affine_3d", "lc2_last_error", "lc2_version",
     "lc2_evaluate_noalloc", "lc2_minimize", "lc2_register", "lc2_params_to_matrix",
+    "lc2_stack_create", "lc2_stack_destroy", "lc2_stack_set_moving", "lc2_stack_add_frame",
+    "lc2_stack_frames", "lc2_stack_frame_context", "lc2_stack_evaluate", "lc2_stack_set_graphs",
+    "lc2_stack_launch_count", "lc2_stack_graph_launches",
 ]
 
 ALGORITHMS = {"direct_l": 1, "bobyqa": 2, "nelder_mead": 3}
@@ -141,6 +144,19 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "lc2_evaluate_noalloc": ([ctypes.c_int, ctypes.POINTER(lc2_geometry),
                                   ctypes.POINTER(lc2_geometry), ctypes.c_int, vp, vp, _fp, vp,
                                   vp], ctypes.c_int),
+        "lc2_stack_create": ([ctypes.POINTER(lc2_geometry), ctypes.c_int, ctypes.c_int,
+                              ctypes.c_int, ctypes.POINTER(vp)], ctypes.c_int),
+        "lc2_stack_destroy": ([vp], ctypes.c_int),
+        "lc2_stack_set_moving": ([vp, _fp], ctypes.c_int),
+        "lc2_stack_add_frame": ([vp, ctypes.POINTER(lc2_geometry), _fp, _fp,
+                                 ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "lc2_stack_frames": ([vp], ctypes.c_int),
+        "lc2_stack_frame_context": ([vp, ctypes.c_int, ctypes.POINTER(vp)], ctypes.c_int),
+        "lc2_stack_evaluate": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _fp, _dp],
+                               ctypes.c_int),
+        "lc2_stack_set_graphs": ([vp, ctypes.c_int], ctypes.c_int),
+        "lc2_stack_launch_count": ([vp], ctypes.c_longlong),
+        "lc2_stack_graph_launches": ([vp], ctypes.c_longlong),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -286,6 +302,85 @@ class Context:
             self._h, m.ctypes.data_as(_fp), ctypes.byref(out),
             *[f[k].ctypes.data_as(_fp) for k in ("U", "M", "G", "sigma", "measure")]))
         return out.value, f
+
+
+class FrameView(Context):
+    """A stack frame's own context (owned by the stack: never destroyed here)."""
+
+    def __init__(self, lib, handle):
+        self._lib = lib
+        self._h = handle
+        self.mode = "2DTo3D"
+        self.matrix_size = 16
+
+    def close(self):
+        self._h = ctypes.c_void_p()
+
+
+class Stack:
+    """A 2D-to-3D frame stack: one moving volume, ultrasound frames of their
+    own sizes, evaluations of (frame, pose) pairs in one launch."""
+
+    def __init__(self, moving_geom: Geometry, patch_size: int, storage: str = "f32",
+                 device: int = 0):
+        lib = load()
+        self._lib = lib
+        self._h = ctypes.c_void_p()
+        g = _geom(moving_geom)
+        _check(lib.lc2_stack_create(ctypes.byref(g), int(patch_size), STORAGE[storage],
+                                    int(device), ctypes.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            self._lib.lc2_stack_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_moving(self, moving: np.ndarray):
+        m = _f32(moving)
+        _check(self._lib.lc2_stack_set_moving(self._h, m.ctypes.data_as(_fp)))
+
+    def add_frame(self, frame_geom: Geometry, virt_spacing, ultrasound: np.ndarray) -> int:
+        g = _geom(frame_geom)
+        vs = _f32(list(virt_spacing) + [1.0] * (3 - len(virt_spacing)))
+        u = _f32(ultrasound)
+        fid = ctypes.c_int()
+        _check(self._lib.lc2_stack_add_frame(self._h, ctypes.byref(g), vs.ctypes.data_as(_fp),
+                                             u.ctypes.data_as(_fp), ctypes.byref(fid)))
+        return fid.value
+
+    def frames(self) -> int:
+        return int(self._lib.lc2_stack_frames(self._h))
+
+    def frame_context(self, frame_id: int) -> "FrameView":
+        h = ctypes.c_void_p()
+        _check(self._lib.lc2_stack_frame_context(self._h, int(frame_id), ctypes.byref(h)))
+        return FrameView(self._lib, h)
+
+    def evaluate(self, frame_ids, mats) -> np.ndarray:
+        ids = np.ascontiguousarray(frame_ids, dtype=np.int32)
+        m = _f32(mats).reshape(-1, 16)
+        if m.shape[0] != ids.shape[0]:
+            raise ValueError("one matrix per frame id")
+        out = np.empty(ids.shape[0], dtype=np.float64)
+        _check(self._lib.lc2_stack_evaluate(self._h, ids.shape[0],
+                                            ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                            m.ctypes.data_as(_fp), out.ctypes.data_as(_dp)))
+        return out
+
+    def set_graphs(self, on: bool):
+        _check(self._lib.lc2_stack_set_graphs(self._h, int(bool(on))))
+
+    def launch_count(self) -> int:
+        return int(self._lib.lc2_stack_launch_count(self._h))
+
+    def graph_launches(self) -> int:
+        return int(self._lib.lc2_stack_graph_launches(self._h))
 
 
 def affine_3d(rot, trans, scale=(1, 1, 1), shear=(0, 0, 0), center=(0, 0, 0), shift=(0, 0, 0)):

@@ -14,6 +14,7 @@
 #include "../../include/lc2.h"
 #include "lc2_kernels.cuh"
 #include "lc2_fused.cuh"
+#include "lc2_list.cuh"
 
 namespace {
 
@@ -65,6 +66,7 @@ struct lc2_context {
 
   // device buffers
   void* d_moving = nullptr;    // storage type, nm
+  bool owns_moving = true;     // false for the frames of a stack (shared volume)
   void* d_static = nullptr;    // hr_moving: U in storage type; hr_fixed: M as float
   float* d_gstatic = nullptr;  // hr_fixed: Sobel(M)
   float* d_scratch = nullptr;  // per-slot warped image (+ Sobel when hr_moving)
@@ -436,8 +438,11 @@ const char* lc2_last_error(void) { return g_err.c_str(); }
 
 const char* lc2_version(void) { return "lc2-gb300 0.1 (sm_103a)"; }
 
-int lc2_create(const lc2_config* cfg, lc2_context** out) {
-  g_err.clear();
+}  // extern "C"
+
+namespace {
+
+int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
   if (!cfg || !out) return fail(LC2_ERR_INVALID_ARGUMENT, "null config or output pointer");
   *out = nullptr;
   if (cfg->mode < LC2_MODE_2D || cfg->mode > LC2_MODE_2DTO3D)
@@ -515,7 +520,8 @@ int lc2_create(const lc2_config* cfg, lc2_context** out) {
   slots = std::min<long long>(slots, 65535 / c->virt.dim[2]);
   c->slots = (int)std::max<long long>(1, slots);
   e = cudaMalloc(&c->d_scratch, per_slot * c->slots);
-  if (e == cudaSuccess) e = cudaMalloc(&c->d_moving, c->nm * elem_size(cfg->storage));
+  c->owns_moving = own_moving;
+  if (e == cudaSuccess && own_moving) e = cudaMalloc(&c->d_moving, c->nm * elem_size(cfg->storage));
   if (e == cudaSuccess)
     e = cudaMalloc(&c->d_static,
                    c->nv * (cfg->high_res_is_moving ? elem_size(cfg->storage) : sizeof(float)));
@@ -538,11 +544,20 @@ int lc2_create(const lc2_config* cfg, lc2_context** out) {
   return LC2_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int lc2_create(const lc2_config* cfg, lc2_context** out) {
+  g_err.clear();
+  return create_context(cfg, true, out);
+}
+
 int lc2_destroy(lc2_context* c) {
   if (!c) return LC2_OK;
   select_device(c);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  cudaFree(c->d_moving);
+  if (c->owns_moving) cudaFree(c->d_moving);
   cudaFree(c->d_static);
   cudaFree(c->d_gstatic);
   cudaFree(c->d_sigma);
@@ -615,31 +630,46 @@ int lc2_kernel_times(lc2_context* c, double ms[3], long long counts[3]) {
   return LC2_OK;
 }
 
-int lc2_set_images(lc2_context* c, const float* fixed, const float* moving) {
-  g_err.clear();
-  if (!c || !fixed || !moving) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
-  LC2_TRY(select_device(c));
-  float fmax = 0.0f, mmax = 0.0f;
-  for (size_t i = 0; i < c->nf; ++i) {
-    if (!std::isfinite(fixed[i])) return fail(LC2_ERR_INVALID_ARGUMENT, "fixed image has NaN/Inf at %zu", i);
-    fmax = std::max(fmax, std::fabs(fixed[i]));
+}  // extern "C"
+
+namespace {
+
+// Largest |value| of a host image; LC2_ERR_INVALID_ARGUMENT on NaN/Inf.
+int image_absmax(const float* img, size_t n, const char* what, float* out) {
+  float mx = 0.0f;
+  for (size_t i = 0; i < n; ++i) {
+    if (!std::isfinite(img[i])) return fail(LC2_ERR_INVALID_ARGUMENT, "%s image has NaN/Inf at %zu", what, i);
+    mx = std::max(mx, std::fabs(img[i]));
   }
-  for (size_t i = 0; i < c->nm; ++i) {
-    if (!std::isfinite(moving[i])) return fail(LC2_ERR_INVALID_ARGUMENT, "moving image has NaN/Inf at %zu", i);
-    mmax = std::max(mmax, std::fabs(moving[i]));
-  }
-  const int storage = c->cfg.storage;
-  // stage both images as float on the device, then convert
+  *out = mx;
+  return LC2_OK;
+}
+
+// Host float image -> device buffer of the storage type (synchronous).
+int upload_image(lc2_context* c, const float* host, size_t n, void* dst, int storage) {
   float* tmp = nullptr;
-  size_t tmp_n = std::max(c->nf, c->nm);
-  LC2_CUDA(cudaMalloc(&tmp, sizeof(float) * tmp_n));
+  LC2_CUDA(cudaMalloc(&tmp, sizeof(float) * n));
   struct Free {
     float* p;
     ~Free() { cudaFree(p); }
   } guard{tmp};
-  // moving volume in storage type
-  LC2_CUDA(cudaMemcpyAsync(tmp, moving, sizeof(float) * c->nm, cudaMemcpyHostToDevice, c->stream));
-  LC2_TRY(convert_to_storage(c, tmp, c->d_moving, c->nm, storage));
+  LC2_CUDA(cudaMemcpyAsync(tmp, host, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+  LC2_TRY(convert_to_storage(c, tmp, dst, n, storage));
+  LC2_CUDA(cudaStreamSynchronize(c->stream));
+  return LC2_OK;
+}
+
+// Everything that depends on the fixed image, given the moving image's
+// largest |value| (its scale enters the fixed-point parameters): the fixed
+// image on the virtual grid, the fixed-point parameters and, for a static
+// ultrasound, the weighting factors and their sum.
+// fmax: the fixed image's largest |value| (image_absmax).
+int set_fixed(lc2_context* c, const float* fixed, float fmax, float mmax) {
+  const int storage = c->cfg.storage;
+  struct Free {
+    float* p;
+    ~Free() { cudaFree(p); }
+  };
   // fixed volume resampled onto the virtual grid through the identity
   // (VirtualToFixed, src/Interpolator/interpolator.cu:526-528)
   float* ffix = nullptr;
@@ -730,6 +760,24 @@ int lc2_set_images(lc2_context* c, const float* fixed, const float* moving) {
   }
   c->ready = true;
   return LC2_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lc2_set_images(lc2_context* c, const float* fixed, const float* moving) {
+  g_err.clear();
+  if (!c || !fixed || !moving) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  if (!c->owns_moving)
+    return fail(LC2_ERR_INVALID_ARGUMENT, "the frames of a stack share the stack's moving volume");
+  LC2_TRY(select_device(c));
+  float fmax = 0.0f, mmax = 0.0f;
+  LC2_TRY(image_absmax(fixed, c->nf, "fixed", &fmax));
+  LC2_TRY(image_absmax(moving, c->nm, "moving", &mmax));
+  c->ready = false;
+  LC2_TRY(upload_image(c, moving, c->nm, c->d_moving, c->cfg.storage));
+  return set_fixed(c, fixed, fmax, mmax);
 }
 
 int lc2_stage_transforms(lc2_context* c, const float* matrices, int count) {
@@ -938,6 +986,366 @@ int lc2_invert_affine_3d(const float in[16], float out[16]) {
   }
   out[12] = out[13] = out[14] = 0.0f;
   out[15] = 1.0f;
+  return LC2_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// 2D-to-3D frame stacks
+// ---------------------------------------------------------------------------
+
+namespace lc2 {
+// LC2 of evaluation k with its own weighting-factor sum.
+__global__ void k_finalize_list(const unsigned long long* __restrict__ acc, int count,
+                                const long long* __restrict__ sigma_sums,
+                                double* __restrict__ out) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  double v = (double)(long long)acc[2 * k] / (double)sigma_sums[k];
+  if (isnan(v) || isinf(v)) v = 0.0;
+  out[k] = v;
+}
+}  // namespace lc2
+
+struct lc2_stack {
+  lc2_config base{};  // mode 2D-to-3D, moving geometry, patch, storage, device
+  size_t nm = 0;
+  void* d_moving = nullptr;
+  float mmax = 0.0f;
+  bool moving_set = false;
+  std::vector<lc2_context*> frames;
+  cudaStream_t stream = nullptr;
+  int sms = 0;
+  // evaluation buffers (device + pinned host), by evaluation in segment order
+  int cap = 0, seg_cap = 0;
+  lc2::Xform* d_xf = nullptr;
+  unsigned long long* d_acc = nullptr;
+  long long* d_sums = nullptr;
+  double* d_out = nullptr;
+  lc2::ListSeg* d_segs = nullptr;
+  lc2::Xform* h_xf = nullptr;
+  long long* h_sums = nullptr;
+  double* h_out = nullptr;
+  lc2::ListSeg* h_segs = nullptr;
+  // CUDA graphs of the launch sequence, keyed by the call's segment layout
+  struct Graph {
+    std::vector<int> key;  // count, then (frame, count) per segment
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+  };
+  std::vector<Graph> graphs;
+  bool use_graphs = true;
+  long long launches = 0, graph_launches = 0;
+};
+
+namespace {
+
+void stack_drop_graphs(lc2_stack* s) {
+  for (auto& g : s->graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.graph) cudaGraphDestroy(g.graph);
+  }
+  s->graphs.clear();
+}
+
+void stack_free_buffers(lc2_stack* s) {
+  cudaFree(s->d_xf);
+  cudaFree(s->d_acc);
+  cudaFree(s->d_sums);
+  cudaFree(s->d_out);
+  cudaFree(s->d_segs);
+  if (s->h_xf) cudaFreeHost(s->h_xf);
+  if (s->h_sums) cudaFreeHost(s->h_sums);
+  if (s->h_out) cudaFreeHost(s->h_out);
+  if (s->h_segs) cudaFreeHost(s->h_segs);
+  s->d_xf = nullptr; s->d_acc = nullptr; s->d_sums = nullptr; s->d_out = nullptr;
+  s->d_segs = nullptr; s->h_xf = nullptr; s->h_sums = nullptr; s->h_out = nullptr;
+  s->h_segs = nullptr;
+  s->cap = s->seg_cap = 0;
+}
+
+// Buffers for `count` evaluations in `nseg` segments. Reallocation moves the
+// buffers the cached graphs read, so it drops them.
+int stack_capacity(lc2_stack* s, int count, int nseg) {
+  if (count <= s->cap && nseg <= s->seg_cap) return LC2_OK;
+  stack_drop_graphs(s);
+  const int ncap = std::max(count, std::max(256, s->cap));
+  const int nseg_cap = std::max(nseg, std::max(64, s->seg_cap));
+  stack_free_buffers(s);
+  LC2_CUDA(cudaMalloc(&s->d_xf, sizeof(lc2::Xform) * ncap));
+  LC2_CUDA(cudaMalloc(&s->d_acc, sizeof(unsigned long long) * 2 * ncap));
+  LC2_CUDA(cudaMalloc(&s->d_sums, sizeof(long long) * ncap));
+  LC2_CUDA(cudaMalloc(&s->d_out, sizeof(double) * ncap));
+  LC2_CUDA(cudaMalloc(&s->d_segs, sizeof(lc2::ListSeg) * nseg_cap));
+  LC2_CUDA(cudaMallocHost(&s->h_xf, sizeof(lc2::Xform) * ncap));
+  LC2_CUDA(cudaMallocHost(&s->h_sums, sizeof(long long) * ncap));
+  LC2_CUDA(cudaMallocHost(&s->h_out, sizeof(double) * ncap));
+  LC2_CUDA(cudaMallocHost(&s->h_segs, sizeof(lc2::ListSeg) * nseg_cap));
+  s->cap = ncap;
+  s->seg_cap = nseg_cap;
+  return LC2_OK;
+}
+
+// The launch sequence of one stack evaluation, on the stack's stream: copies
+// of the transforms, segments and weighting-factor sums, the work-list
+// kernel, the per-evaluation ratio and the copy of the results.
+int stack_enqueue(lc2_stack* s, int count, int nseg, long long units) {
+  cudaStream_t st = s->stream;
+  LC2_CUDA(cudaMemcpyAsync(s->d_xf, s->h_xf, sizeof(lc2::Xform) * count, cudaMemcpyHostToDevice, st));
+  LC2_CUDA(cudaMemcpyAsync(s->d_segs, s->h_segs, sizeof(lc2::ListSeg) * nseg, cudaMemcpyHostToDevice, st));
+  LC2_CUDA(cudaMemcpyAsync(s->d_sums, s->h_sums, sizeof(long long) * count, cudaMemcpyHostToDevice, st));
+  LC2_CUDA(cudaMemsetAsync(s->d_acc, 0, sizeof(unsigned long long) * 2 * count, st));
+  lc2::ListLaunch L;
+  L.segs = s->d_segs;
+  L.nseg = nseg;
+  L.units = units;
+  L.xf = s->d_xf;
+  L.acc = s->d_acc;
+  L.r = s->base.patch_size;
+  L.wnd = 3;
+  L.sms = s->sms;
+  L.stream = st;
+  cudaError_t e;
+  if (s->base.storage == LC2_STORE_F16)
+    e = lc2::list_launch<__half>(L);
+  else if (s->base.storage == LC2_STORE_BF16)
+    e = lc2::list_launch<__nv_bfloat16>(L);
+  else
+    e = lc2::list_launch<float>(L);
+  LC2_CUDA(e);
+  lc2::k_finalize_list<<<(count + 127) / 128, 128, 0, st>>>(s->d_acc, count, s->d_sums, s->d_out);
+  LC2_CUDA(cudaGetLastError());
+  LC2_CUDA(cudaMemcpyAsync(s->h_out, s->d_out, sizeof(double) * count, cudaMemcpyDeviceToHost, st));
+  return LC2_OK;
+}
+
+int stack_select_device(const lc2_stack* s) {
+  int cur = -1;
+  LC2_CUDA(cudaGetDevice(&cur));
+  if (cur != s->base.device) LC2_CUDA(cudaSetDevice(s->base.device));
+  return LC2_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lc2_stack_create(const lc2_geometry* moving, int patch_size, int storage, int device,
+                     lc2_stack** out) {
+  g_err.clear();
+  if (!moving || !out) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (!finite_geom(*moving))
+    return fail(LC2_ERR_INVALID_ARGUMENT, "geometry needs dims >= 1, finite spacing > 0 and origin");
+  if (storage < LC2_STORE_F32 || storage > LC2_STORE_BF16)
+    return fail(LC2_ERR_INVALID_ARGUMENT, "unknown storage %d", storage);
+  if (patch_size < 1 || patch_size > 12)
+    return fail(LC2_ERR_UNSUPPORTED, "patch size %d outside [1, 12] for 2D patches", patch_size);
+  lc2_stack* s = new (std::nothrow) lc2_stack();
+  if (!s) return fail(LC2_ERR_OUT_OF_MEMORY, "host allocation failed");
+  s->base.mode = LC2_MODE_2DTO3D;
+  s->base.moving = *moving;
+  s->base.patch_size = patch_size;
+  s->base.high_res_is_moving = 1;
+  s->base.storage = storage;
+  s->base.max_batch = 1;
+  s->base.device = device;
+  s->nm = (size_t)moving->dim[0] * moving->dim[1] * moving->dim[2];
+  int st = stack_select_device(s);
+  cudaError_t e = cudaSuccess;
+  if (st == LC2_OK) e = cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, device);
+  if (st == LC2_OK && e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (st == LC2_OK && e == cudaSuccess) e = cudaMalloc(&s->d_moving, s->nm * elem_size(storage));
+  if (st != LC2_OK || e != cudaSuccess) {
+    std::string msg = st != LC2_OK ? g_err : std::string(cudaGetErrorString(e));
+    lc2_stack_destroy(s);
+    return fail(st != LC2_OK ? st : LC2_ERR_OUT_OF_MEMORY, "stack: %s", msg.c_str());
+  }
+  *out = s;
+  return LC2_OK;
+}
+
+int lc2_stack_destroy(lc2_stack* s) {
+  if (!s) return LC2_OK;
+  stack_select_device(s);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (lc2_context* f : s->frames) lc2_destroy(f);
+  stack_drop_graphs(s);
+  stack_free_buffers(s);
+  cudaFree(s->d_moving);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return LC2_OK;
+}
+
+int lc2_stack_set_moving(lc2_stack* s, const float* moving) {
+  g_err.clear();
+  if (!s || !moving) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  if (s->moving_set) return fail(LC2_ERR_INVALID_ARGUMENT, "the stack's moving volume is already set");
+  LC2_TRY(stack_select_device(s));
+  float mmax = 0.0f;
+  LC2_TRY(image_absmax(moving, s->nm, "moving", &mmax));
+  // staged through a temporary one-slot context for its conversion kernels
+  float* tmp = nullptr;
+  LC2_CUDA(cudaMalloc(&tmp, sizeof(float) * s->nm));
+  struct Free {
+    float* p;
+    ~Free() { cudaFree(p); }
+  } guard{tmp};
+  LC2_CUDA(cudaMemcpyAsync(tmp, moving, sizeof(float) * s->nm, cudaMemcpyHostToDevice, s->stream));
+  lc2_context conv;  // only its stream and launch counter are used
+  conv.stream = s->stream;
+  LC2_TRY(convert_to_storage(&conv, tmp, s->d_moving, s->nm, s->base.storage));
+  LC2_CUDA(cudaStreamSynchronize(s->stream));
+  s->launches += conv.launches;
+  s->mmax = mmax;
+  s->moving_set = true;
+  return LC2_OK;
+}
+
+int lc2_stack_add_frame(lc2_stack* s, const lc2_geometry* frame, const float virtual_spacing[3],
+                        const float* ultrasound, int* frame_id) {
+  g_err.clear();
+  if (!s || !frame || !virtual_spacing || !ultrasound || !frame_id)
+    return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  if (!s->moving_set) return fail(LC2_ERR_NOT_READY, "set the stack's moving volume first");
+  if (frame->dim[2] != 1) return fail(LC2_ERR_INVALID_ARGUMENT, "a frame has dim[2] = 1");
+  LC2_TRY(stack_select_device(s));
+  lc2_config cfg = s->base;
+  cfg.fixed = *frame;
+  for (int a = 0; a < 3; ++a) cfg.virtual_spacing[a] = virtual_spacing[a];
+  lc2_context* c = nullptr;
+  LC2_TRY(create_context(&cfg, false, &c));
+  c->d_moving = s->d_moving;
+  float fmax = 0.0f;
+  int st = image_absmax(ultrasound, c->nf, "ultrasound", &fmax);
+  if (st == LC2_OK) st = set_fixed(c, ultrasound, fmax, s->mmax);
+  if (st != LC2_OK) {
+    std::string msg = g_err;
+    lc2_destroy(c);
+    g_err = msg;
+    return st;
+  }
+  s->launches += c->launches;
+  *frame_id = (int)s->frames.size();
+  s->frames.push_back(c);
+  return LC2_OK;
+}
+
+int lc2_stack_frames(const lc2_stack* s) { return s ? (int)s->frames.size() : 0; }
+
+int lc2_stack_frame_context(lc2_stack* s, int frame_id, lc2_context** ctx) {
+  if (!s || !ctx) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  if (frame_id < 0 || frame_id >= (int)s->frames.size())
+    return fail(LC2_ERR_INVALID_ARGUMENT, "no frame %d", frame_id);
+  *ctx = s->frames[frame_id];
+  return LC2_OK;
+}
+
+int lc2_stack_set_graphs(lc2_stack* s, int on) {
+  if (!s) return fail(LC2_ERR_INVALID_ARGUMENT, "null stack");
+  s->use_graphs = on != 0;
+  return LC2_OK;
+}
+
+long long lc2_stack_launch_count(const lc2_stack* s) { return s ? s->launches : 0; }
+long long lc2_stack_graph_launches(const lc2_stack* s) { return s ? s->graph_launches : 0; }
+
+int lc2_stack_evaluate(lc2_stack* s, int count, const int* frame_ids, const float* matrices,
+                       double* lc2_out) {
+  g_err.clear();
+  if (!s) return fail(LC2_ERR_INVALID_ARGUMENT, "null stack");
+  if (count < 0 || (count > 0 && (!frame_ids || !matrices || !lc2_out)))
+    return fail(LC2_ERR_INVALID_ARGUMENT, "bad evaluation request");
+  if (count == 0) return LC2_OK;
+  const int nf = (int)s->frames.size();
+  for (int k = 0; k < count; ++k) {
+    if (frame_ids[k] < 0 || frame_ids[k] >= nf)
+      return fail(LC2_ERR_INVALID_ARGUMENT, "evaluation %d names frame %d of %d", k, frame_ids[k], nf);
+    for (int i = 0; i < 16; ++i)
+      if (!std::isfinite(matrices[(size_t)k * 16 + i]))
+        return fail(LC2_ERR_INVALID_ARGUMENT, "transform %d has NaN/Inf", k);
+  }
+  LC2_TRY(stack_select_device(s));
+  // evaluations grouped by frame (stable), one segment per frame
+  std::vector<int> order(count);
+  for (int k = 0; k < count; ++k) order[k] = k;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return frame_ids[a] < frame_ids[b]; });
+  std::vector<int> key{count};
+  int nseg = 0;
+  for (int k = 0; k < count; ++k)
+    if (k == 0 || frame_ids[order[k]] != frame_ids[order[k - 1]]) ++nseg;
+  LC2_TRY(stack_capacity(s, count, nseg));
+  long long units = 0;
+  int seg = -1;
+  for (int k = 0; k < count; ++k) {
+    const int f = frame_ids[order[k]];
+    const lc2_context* c = s->frames[f];
+    if (k == 0 || f != frame_ids[order[k - 1]]) {
+      ++seg;
+      lc2::ListSeg& S = s->h_segs[seg];
+      S.mov = s->d_moving;
+      S.ust = c->d_static;
+      S.sig = c->d_sigma;
+      S.P = c->fp;
+      S.P.ntx = (c->virt.dim[0] + 31) / 32;
+      S.P.zchunk = 1;
+      S.ntiles = S.P.ntx * ((c->virt.dim[1] + lc2::kListTY - 1) / lc2::kListTY);
+      S.count = 0;
+      S.eval0 = k;
+      S.pad_ = 0;
+      S.unit0 = units;
+      key.push_back(f);
+      key.push_back(0);
+    }
+    lc2::ListSeg& S = s->h_segs[seg];
+    ++S.count;
+    ++key.back();
+    units += S.ntiles;
+    build_xform(3, c->virt, c->cfg.moving, matrices + (size_t)order[k] * 16, &s->h_xf[k]);
+    s->h_sums[k] = c->sigma_sum;
+  }
+  if (s->use_graphs) {
+    lc2_stack::Graph* g = nullptr;
+    for (auto& cand : s->graphs)
+      if (cand.key == key) g = &cand;
+    if (!g) {
+      lc2_stack::Graph ng;
+      ng.key = key;
+      LC2_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeRelaxed));
+      int st = stack_enqueue(s, count, nseg, units);
+      cudaGraph_t graph = nullptr;
+      cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+      if (st != LC2_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return st;
+      }
+      LC2_CUDA(e);
+      ng.graph = graph;
+      e = cudaGraphInstantiate(&ng.exec, graph, 0);
+      if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        LC2_CUDA(e);
+      }
+      if (s->graphs.size() >= 16) {  // keep the cache small
+        cudaGraphExecDestroy(s->graphs.front().exec);
+        cudaGraphDestroy(s->graphs.front().graph);
+        s->graphs.erase(s->graphs.begin());
+      }
+      s->graphs.push_back(ng);
+      g = &s->graphs.back();
+    }
+    LC2_CUDA(cudaGraphLaunch(g->exec, s->stream));
+    ++s->graph_launches;
+    s->launches += 2;
+  } else {
+    LC2_TRY(stack_enqueue(s, count, nseg, units));
+    s->launches += 2;
+  }
+  LC2_CUDA(cudaStreamSynchronize(s->stream));
+  for (int k = 0; k < count; ++k) lc2_out[order[k]] = s->h_out[k];
   return LC2_OK;
 }
 

@@ -226,6 +226,97 @@ __device__ __forceinline__ float fused_sobel(const float* mc, const float* S, co
   return sqrtf(gx * gx + gy * gy);
 }
 
+// Per-tile transform state in shared memory.
+struct TileShared {
+  double base[3];  // resampled-region origin in moving pixels
+  int ib[3];       // its integer part
+  float fb[3];     // and fraction
+  float A[9];      // moving-pixel step per region pixel
+};
+
+// One 32 x TY output tile of a 2D window (2D, or a 2D-to-3D frame when
+// WND = 3): resample the halo region, Sobel, limbs, x/y window passes and the
+// clipped measures. Returns this thread's fixed-point measure sum; the caller
+// reduces it. Ends with the shared planes still in use: callers that reuse
+// them for another tile must synchronise first.
+template <int WND, typename TM, typename TS, int TY, int R>
+__device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
+                                                   const TS* __restrict__ Ust,
+                                                   const float* __restrict__ sig,
+                                                   const FusedParams& P, const Xform* X, int tile,
+                                                   unsigned char* smem_raw, TileShared& T,
+                                                   float* __restrict__ out_measure) {
+  using G = FusedGeom<2, TY, R>;
+  constexpr int NT = G::NT;
+  constexpr size_t PA = (size_t)G::HY * G::HXP;
+  float* mc = reinterpret_cast<float*>(smem_raw);
+  int* A = reinterpret_cast<int*>(smem_raw + G::OFF_A);
+  const int tid = threadIdx.x;
+  const int ntx = P.ntx;
+  const int x0 = (tile % ntx) * 32, y0 = (tile / ntx) * TY;
+  const int gx0 = x0 - R - 1, gy0 = y0 - R - 1;
+  if (tid == 0) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double p = X->A[3 * a + 0] * gx0 + X->A[3 * a + 1] * gy0 + X->b[a];
+      const double fl = floor(p);
+      T.base[a] = p;
+      T.ib[a] = (int)fl;
+      T.fb[a] = (float)(p - fl);
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) T.A[i] = (float)X->A[i];
+  }
+  __syncthreads();
+  for (int i = tid; i < G::NPW; i += NT) {
+    const int py = i / G::PW, px = i - py * G::PW;
+    const int gx = gx0 + px, gy = gy0 + py;
+    float v = 0.0f;
+    if (gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy)
+      v = fused_sample<WND, TM>(mov, P, T.A, T.ib, T.fb, px, py);
+    mc[i] = v;
+  }
+  __syncthreads();
+  for (int p = tid; p < G::NP; p += NT) {
+    const int hy = p / G::HX, hx = p - hy * G::HX;
+    const int gx = x0 - R + hx, gy = y0 - R + hy;
+    const int c = (hy + 1) * G::PW + hx + 1;
+    const float m = mc[c];
+    const float g = fused_sobel<2, G::PW>(mc, nullptr, nullptr, c);
+    float u = 0.0f;
+    if (gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy) u = ldf(Ust, (size_t)gy * P.vx + gx);
+    int L[kLimbs];
+    fused_limbs(quant(u, P.qu), quant(m, P.qm), quant(g, P.qg), P.kbits, L);
+    int* a = A + hy * G::HXP + hx;
+#pragma unroll
+    for (int k = 0; k < kLimbs; ++k) a[k * PA] = L[k];
+  }
+  __syncthreads();
+  fused_xy<2, TY, R>(A);
+  long long acc_m = 0;
+  const int ox = tid & 31, oy = tid >> 5;
+  const int x = x0 + ox, y = y0 + oy;
+  if (x < P.vx && y < P.vy) {
+    const size_t gi = (size_t)y * P.vx + x;
+    const float sg = __ldg(sig + gi);
+    float m = 0.0f;
+    if (sg > 0.0f) {
+      const int* a = A + oy * G::HXP + ox;
+      int L[kLimbs];
+#pragma unroll
+      for (int k = 0; k < kLimbs; ++k) L[k] = a[k * PA];
+      long long Sx[5];
+#pragma unroll
+      for (int i = 0; i < 5; ++i)
+        Sx[i] = (long long)L[4 + 2 * i] * (1LL << P.kbits) + (long long)L[3 + 2 * i];
+      m = fused_solve(P, sg, L[0], L[1], L[2], Sx[0], Sx[1], Sx[2], Sx[3], Sx[4]);
+      acc_m = __float2int_rn(m * P.sum_scale);
+    }
+    if (out_measure) out_measure[gi] = m;
+  }
+  return acc_m;
+}
+
 template <int ND, int WND, typename TM, typename TS, int TY, int R>
 __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* __restrict__ mov,
                                                       const TS* __restrict__ Ust,
@@ -301,34 +392,9 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
   };
 
   if constexpr (ND == 2) {
-    set_base(0);
-    __syncthreads();
-    for (int i = tid; i < G::NPW; i += NT) {
-      const int py = i / G::PW, px = i - py * G::PW;
-      const int gx = gx0 + px, gy = gy0 + py;
-      float v = 0.0f;
-      if (gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy)
-        v = fused_sample<WND, TM>(mov, P, s_A, s_ib, s_fb, px, py);
-      mc[i] = v;
-    }
-    __syncthreads();
-    for (int p = tid; p < G::NP; p += NT) {
-      const int hy = p / G::HX, hx = p - hy * G::HX;
-      const int gx = x0 - R + hx, gy = y0 - R + hy;
-      const int c = (hy + 1) * G::PW + hx + 1;
-      const float m = mc[c];
-      const float g = fused_sobel<2, G::PW>(mc, S, D, c);
-      float u = 0.0f;
-      if (gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy) u = ldf(Ust, (size_t)gy * P.vx + gx);
-      int L[kLimbs];
-      fused_limbs(quant(u, P.qu), quant(m, P.qm), quant(g, P.qg), P.kbits, L);
-      int* a = A + hy * G::HXP + hx;
-#pragma unroll
-      for (int k = 0; k < kLimbs; ++k) a[k * PA] = L[k];
-    }
-    __syncthreads();
-    fused_xy<ND, TY, R>(A);
-    solve_out(0);
+    __shared__ TileShared T;
+    acc_m = fused_tile_2d<WND, TM, TS, TY, R>(mov, Ust, sig, P, X, tile, smem_raw, T,
+                                              slot == 0 ? out_measure : nullptr);
   } else {
     // ---- 3D: z-marching over output slices [zb, ze) ----
     const int zb = blockIdx.z * P.zchunk;

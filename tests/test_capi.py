@@ -67,3 +67,18 @@ def test_null_context_calls_fail_cleanly():
     m = (ctypes.c_float * 16)()
     assert lib.lc2_evaluate(None, m, ctypes.byref(out)) != 0
     assert lib.lc2_destroy(None) == 0
+
+
+def test_stack_rejects_bad_arguments_without_gpu():
+    lib = capi.load()
+    h = ctypes.c_void_p()
+    g = capi._geom(Geometry((16, 16, 16), (1, 1, 1), (0, 0, 0)))
+    assert lib.lc2_stack_create(None, 3, 0, 0, ctypes.byref(h)) == 1
+    assert lib.lc2_stack_create(ctypes.byref(g), 0, 0, 0, ctypes.byref(h)) == 6
+    assert lib.lc2_stack_create(ctypes.byref(g), 13, 0, 0, ctypes.byref(h)) == 6
+    assert lib.lc2_stack_create(ctypes.byref(g), 3, 7, 0, ctypes.byref(h)) == 1
+    bad = capi._geom(Geometry((16, 16, 16), (1, -1, 1), (0, 0, 0)))
+    assert lib.lc2_stack_create(ctypes.byref(bad), 3, 0, 0, ctypes.byref(h)) == 1
+    assert lib.lc2_stack_evaluate(None, 1, None, None, None) == 1
+    assert lib.lc2_stack_frames(None) == 0
+    assert lib.lc2_stack_destroy(None) == 0
