@@ -56,6 +56,10 @@ def parse():
     ap.add_argument("--plain-evals", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=48)
+    ap.add_argument("--serve-rate", type=float, default=4.0, help="Poisson arrivals per second")
+    ap.add_argument("--serve-active", type=int, default=8)
     return ap.parse_args()
 
 
@@ -156,6 +160,88 @@ def cpu_port(case, mats, seconds: float, storage: str):
         if el >= seconds and done >= 2:
             break
     return done / el, done, el
+
+
+def _registration(case, rng):
+    """Registration settings of one served request: DIRECT on the translation,
+    then two local rounds to xtol 1e-6, from a seeded start near identity."""
+    c = case.fixed_geom.center()
+    if case.mode == "2D":
+        init = [rng.uniform(-2, 2), rng.uniform(-2, 2), rng.uniform(-2, 2), 1, 1, 0]
+        lo = [-12, -12, -10, 0.9, 0.9, -0.06]
+        hi = [12, 12, 10, 1.1, 1.1, 0.06]
+    else:
+        init = list(rng.uniform(-2, 2, 6)) + [1, 1, 1, 0, 0, 0]
+        lo = [-12, -12, -12, -10, -10, -10, 0.9, 0.9, 0.9, -0.05, -0.05, -0.05]
+        hi = [12, 12, 12, 10, 10, 10, 1.1, 1.1, 1.1, 0.05, 0.05, 0.05]
+    return dict(initial=init, lower=lo, upper=hi, center=c, direct_entries=["translation"],
+                direct_maxeval=50, round_maxeval=400,
+                rounds=[(["translation", "rotation"], 1e-6),
+                        (["translation", "rotation", "scale", "shear"], 1e-6)])
+
+
+def serve_leg(args, main_case, device):
+    """Serving: Poisson arrivals of whole registrations, mix 40% 2D 256^2,
+    30% 3D 128^3 -> 96^3, 20% 3D 256^3 FP16 (the main workload's volumes),
+    10% 2D-to-3D stacks of 16 uneven frames cut from the 256^3 MR. Returns the
+    latency percentiles (submit -> result) and the request rate."""
+    import numpy as np
+
+    from lc2registration_gb300 import capi, synth
+
+    rng = np.random.default_rng(4242)
+    pools = {
+        "2d_256": [synth.case_2d(seed=s, size=256, r=3) for s in (101, 102)],
+        "3d_128_96": [synth.case_3d(seed=s, mr_size=128, us_size=96, r=3) for s in (103, 104)],
+        "3d_256_f16": [main_case],
+        "stack16": [synth.frame_stack(main_case.moving, main_case.moving_geom, 16, seed=105,
+                                      spacing=0.5, r=3)],
+    }
+    kinds = rng.choice(list(pools), size=args.serve_requests, p=[0.4, 0.3, 0.2, 0.1])
+    srv = capi.Server(budget_bytes=0, max_active=args.serve_active, device=device)
+
+    def submit(case, storage):
+        cfg = capi.make_config(case.mode, case.fixed_geom, case.moving_geom, case.virt_spacing,
+                               case.r, case.hr_moving, storage, device=device)
+        return srv.submit(cfg, case.fixed, case.moving, **_registration(case, rng))
+
+    sent = []  # (kind, [tickets], submit time)
+    t0 = time.perf_counter()
+    for k in kinds:
+        pool = pools[k]
+        item = pool[int(rng.integers(len(pool)))]
+        if k == "stack16":
+            tickets = [submit(f, "f32") for f in item]
+        else:
+            tickets = [submit(item, "f16" if k == "3d_256_f16" else "f32")]
+        sent.append((k, tickets))
+        time.sleep(rng.exponential(1.0 / args.serve_rate))
+    lat = {k: [] for k in pools}
+    evals = 0
+    for k, tickets in sent:
+        rs = [srv.poll(t) for t in tickets]
+        for r in rs:
+            assert r["status"] == 0, r["message"]
+            evals += r["evaluations"]
+        lat[k].append(max(r["total_ms"] for r in rs))
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    allv = np.array([v for vs in lat.values() for v in vs])
+
+    def pct(v, q):
+        return float(np.percentile(v, q, method="inverted_cdf")) if len(v) else None
+    return {
+        "requests": len(sent), "rate_offered": args.serve_rate,
+        "requests_per_s": len(sent) / wall, "evals_per_s": evals / wall,
+        "p50_ms": pct(allv, 50), "p95_ms": pct(allv, 95), "p99_ms": pct(allv, 99),
+        "by_kind_p50_ms": {k: pct(np.array(v), 50) for k, v in lat.items()},
+        "by_kind_count": {k: len(v) for k, v in lat.items()},
+        "max_active": args.serve_active, "peak_active": st["peak_active"],
+        "peak_device_bytes": st["peak_bytes"],
+        "mix": "40% 2D 256^2 r3, 30% 3D 128^3->96^3 r3, 20% 3D 256^3 f16 r4, 10% 2D-to-3D "
+               "stacks of 16 frames (sides 128-512 at 0.5 mm) r3; DIRECT + 2 rounds to xtol 1e-6",
+    }
 
 
 def run_reference(args):
@@ -315,6 +401,10 @@ def main():
                "sample": f"{n} full {args.size}^3 evaluations of the FP64 oracle over "
                          f"{el:.1f} s (OpenMP, all host cores); the reference has no CPU LC2 path"}
 
+    serve = None
+    if rank == 0 and not args.no_serve:
+        serve = serve_leg(args, case, local)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -331,6 +421,7 @@ def main():
                     "d2h_bytes_per_step": K * 8},
             "plain": {"value": plain_eps, "unit": UNIT, "evals": P,
                       "batched_over_plain": value / world / plain_eps},
+            "serve": serve,
             "gpu_launches": launches,
             "clocks": clk.summary(),
             "lc2_true_transform": float(ctx.evaluate(case.true_mat)),

@@ -228,6 +228,62 @@ int lc2_register(lc2_context* ctx, const lc2_registration* reg, lc2_registration
 int lc2_params_to_matrix(int mode, const double* params, const float center[3],
                          const float shift[3], float* matrix);
 
+/* ---- Serving ----
+ * A request loop for whole registrations (the reference registers one
+ * request per process, src/mainRegistrationTool/main.cu:728-801). Requests
+ * are admitted in arrival order while their device memory fits the budget
+ * and fewer than max_active are running; each admitted request runs on its
+ * own worker thread with its own context and CUDA stream, so the kernels of
+ * concurrent requests overlap on the GPU, and a request's images, weighting
+ * factors and optimizer state stay resident until it completes. Results
+ * are identical to the same request registered alone (lc2_register). */
+typedef struct lc2_server lc2_server;
+typedef struct {
+    size_t hbm_budget_bytes; /* device bytes admitted requests may hold; 0 = 80% of free memory */
+    int max_active;          /* registrations in flight (worker threads); 0 = 8 */
+    int device;              /* CUDA device of every request */
+} lc2_server_config;
+typedef struct {
+    lc2_config config;       /* images, patch, storage (config.device is replaced by the server's) */
+    const float* fixed;      /* host images, copied by lc2_server_submit */
+    const float* moving;
+    /* optimizer settings; with registration.lc2_of_matrices set the request
+     * runs that host objective and touches no GPU */
+    lc2_registration registration;
+} lc2_request;
+typedef struct {
+    int status;                      /* lc2_status of the registration */
+    char message[160];               /* lc2_last_error() of a failed request */
+    lc2_registration_result result;
+    double queue_ms, run_ms, total_ms; /* submit->admission, admission->done, submit->done */
+    size_t device_bytes;             /* budget the request held while running */
+    long long admission;             /* admission order 0, 1, ... */
+} lc2_request_result;
+typedef struct {
+    long long submitted, completed, failed;
+    int queued, active, peak_active;
+    size_t budget_bytes, bytes_in_use, peak_bytes;
+    double p50_ms, p95_ms, p99_ms, mean_ms; /* total latency of completed requests */
+    double elapsed_s;                /* since creation or the last reset */
+} lc2_server_stats;
+
+/* Device bytes a context of this configuration holds (*held) and at most
+ * while lc2_set_images runs (*peak, may be NULL). No device work. */
+int lc2_context_bytes(const lc2_config* cfg, size_t* held, size_t* peak);
+int lc2_server_create(const lc2_server_config* cfg, lc2_server** out);
+/* Queues a request; *ticket identifies it. LC2_ERR_OUT_OF_MEMORY when the
+ * request alone exceeds the budget. */
+int lc2_server_submit(lc2_server* s, const lc2_request* req, long long* ticket);
+/* Waits up to wait_ms (-1 = no limit) for the request; LC2_ERR_NOT_READY
+ * while it is queued or running. A completed result is returned once. */
+int lc2_server_poll(lc2_server* s, long long ticket, int wait_ms, lc2_request_result* out);
+/* Waits up to wait_ms (-1 = no limit) until nothing is queued or running. */
+int lc2_server_drain(lc2_server* s, int wait_ms);
+int lc2_server_get_stats(lc2_server* s, lc2_server_stats* out);
+int lc2_server_reset_stats(lc2_server* s);
+/* Finishes running requests, drops queued ones, joins the workers. */
+int lc2_server_destroy(lc2_server* s);
+
 /* ---- 2D-to-3D frame stacks ----
  * One MR/CT volume against many ultrasound frames of their own sizes and
  * geometries, with any number of candidate poses per frame, evaluated in one

@@ -38,7 +38,9 @@ EXPORTED = [
     "lc2_evaluate_noalloc", "lc2_minimize", "lc2_register", "lc2_params_to_matrix",
     "lc2_stack_create", "lc2_stack_destroy", "lc2_stack_set_moving", "lc2_stack_add_frame",
     "lc2_stack_frames", "lc2_stack_frame_context", "lc2_stack_evaluate", "lc2_stack_set_graphs",
-    "lc2_stack_launch_count", "lc2_stack_graph_launches",
+    "lc2_stack_launch_count", "lc2_stack_graph_launches", "lc2_context_bytes",
+    "lc2_server_create", "lc2_server_submit", "lc2_server_poll", "lc2_server_drain",
+    "lc2_server_get_stats", "lc2_server_reset_stats", "lc2_server_destroy",
 ]
 
 ALGORITHMS = {"direct_l": 1, "bobyqa": 2, "nelder_mead": 3}
@@ -95,6 +97,33 @@ class lc2_config(ctypes.Structure):
                 ("virtual_spacing", ctypes.c_float * 3), ("patch_size", ctypes.c_int),
                 ("high_res_is_moving", ctypes.c_int), ("storage", ctypes.c_int),
                 ("max_batch", ctypes.c_int), ("device", ctypes.c_int)]
+
+
+class lc2_server_config(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("max_active", ctypes.c_int),
+                ("device", ctypes.c_int)]
+
+
+class lc2_request(ctypes.Structure):
+    _fields_ = [("config", lc2_config), ("fixed", ctypes.POINTER(ctypes.c_float)),
+                ("moving", ctypes.POINTER(ctypes.c_float)), ("registration", lc2_registration)]
+
+
+class lc2_request_result(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("message", ctypes.c_char * 160),
+                ("result", lc2_registration_result), ("queue_ms", ctypes.c_double),
+                ("run_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
+                ("device_bytes", ctypes.c_size_t), ("admission", ctypes.c_longlong)]
+
+
+class lc2_server_stats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_longlong), ("completed", ctypes.c_longlong),
+                ("failed", ctypes.c_longlong), ("queued", ctypes.c_int), ("active", ctypes.c_int),
+                ("peak_active", ctypes.c_int), ("budget_bytes", ctypes.c_size_t),
+                ("bytes_in_use", ctypes.c_size_t), ("peak_bytes", ctypes.c_size_t),
+                ("p50_ms", ctypes.c_double), ("p95_ms", ctypes.c_double),
+                ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
+                ("elapsed_s", ctypes.c_double)]
 
 
 _fp = ctypes.POINTER(ctypes.c_float)
@@ -157,6 +186,18 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "lc2_stack_set_graphs": ([vp, ctypes.c_int], ctypes.c_int),
         "lc2_stack_launch_count": ([vp], ctypes.c_longlong),
         "lc2_stack_graph_launches": ([vp], ctypes.c_longlong),
+        "lc2_context_bytes": ([ctypes.POINTER(lc2_config), ctypes.POINTER(ctypes.c_size_t),
+                               ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+        "lc2_server_create": ([ctypes.POINTER(lc2_server_config), ctypes.POINTER(vp)],
+                              ctypes.c_int),
+        "lc2_server_submit": ([vp, ctypes.POINTER(lc2_request), ctypes.POINTER(ctypes.c_longlong)],
+                              ctypes.c_int),
+        "lc2_server_poll": ([vp, ctypes.c_longlong, ctypes.c_int,
+                             ctypes.POINTER(lc2_request_result)], ctypes.c_int),
+        "lc2_server_drain": ([vp, ctypes.c_int], ctypes.c_int),
+        "lc2_server_get_stats": ([vp, ctypes.POINTER(lc2_server_stats)], ctypes.c_int),
+        "lc2_server_reset_stats": ([vp], ctypes.c_int),
+        "lc2_server_destroy": ([vp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -184,6 +225,31 @@ def _f32(a) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.float32)
 
 
+def make_config(mode: str, fixed_geom: Geometry, moving_geom: Geometry,
+                virt_spacing: Sequence[float], patch_size: int, high_res_is_moving: bool = True,
+                storage: str = "f32", max_batch: int = 0, device: int = 0) -> lc2_config:
+    cfg = lc2_config()
+    cfg.mode = MODES[mode]
+    cfg.fixed = _geom(fixed_geom)
+    cfg.moving = _geom(moving_geom)
+    vs = list(virt_spacing) + [1.0] * (3 - len(virt_spacing))
+    for a in range(3):
+        cfg.virtual_spacing[a] = float(vs[a])
+    cfg.patch_size = int(patch_size)
+    cfg.high_res_is_moving = int(bool(high_res_is_moving))
+    cfg.storage = STORAGE[storage]
+    cfg.max_batch = int(max_batch)
+    cfg.device = int(device)
+    return cfg
+
+
+def context_bytes(cfg: lc2_config):
+    """(held, peak) device bytes of a context of this configuration."""
+    held, peak = ctypes.c_size_t(), ctypes.c_size_t()
+    _check(load().lc2_context_bytes(ctypes.byref(cfg), ctypes.byref(held), ctypes.byref(peak)))
+    return held.value, peak.value
+
+
 class Context:
     """One LC2 evaluation context (fixed + moving image on one GPU)."""
 
@@ -191,18 +257,8 @@ class Context:
                  virt_spacing: Sequence[float], patch_size: int, high_res_is_moving: bool = True,
                  storage: str = "f32", max_batch: int = 0, device: int = 0):
         lib = load()
-        cfg = lc2_config()
-        cfg.mode = MODES[mode]
-        cfg.fixed = _geom(fixed_geom)
-        cfg.moving = _geom(moving_geom)
-        vs = list(virt_spacing) + [1.0] * (3 - len(virt_spacing))
-        for a in range(3):
-            cfg.virtual_spacing[a] = float(vs[a])
-        cfg.patch_size = int(patch_size)
-        cfg.high_res_is_moving = int(bool(high_res_is_moving))
-        cfg.storage = STORAGE[storage]
-        cfg.max_batch = int(max_batch)
-        cfg.device = int(device)
+        cfg = make_config(mode, fixed_geom, moving_geom, virt_spacing, patch_size,
+                          high_res_is_moving, storage, max_batch, device)
         self.mode = mode
         self.matrix_size = 9 if mode == "2D" else 16
         self._h = ctypes.c_void_p()
@@ -464,6 +520,31 @@ def register(ctx, initial, lower, upper, center, shift=(0.0, 0.0, 0.0), direct_e
     evaluations, launches)."""
     lib = load()
     mode = mode or ctx.mode
+    err = []
+    keep = []
+    reg = make_registration(mode, initial, lower, upper, center, shift, direct_entries,
+                            direct_maxeval, rounds, round_maxeval, local_algorithm,
+                            lc2_of_matrices, observer, err, keep)
+    out = lc2_registration_result()
+    st = lib.lc2_register(ctx.handle if ctx is not None else None, ctypes.byref(reg),
+                          ctypes.byref(out))
+    if err:
+        raise err[0]
+    _check(st)
+    n = 6 if mode == "2D" else 12
+    return dict(params=np.array(out.params[:n]), lc2=out.lc2, evaluations=out.evaluations,
+                launches=out.launches)
+
+
+def make_registration(mode, initial, lower, upper, center, shift=(0.0, 0.0, 0.0),
+                      direct_entries=(), direct_maxeval: int = 50, rounds=(),
+                      round_maxeval: int = 0, local_algorithm: str = "bobyqa",
+                      lc2_of_matrices=None, observer=None, err=None, keep=None):
+    """An lc2_registration struct. Python callbacks append their exceptions to
+    err; the ctypes callback objects are appended to keep, which the caller
+    holds while the struct is in use."""
+    err = [] if err is None else err
+    keep = [] if keep is None else keep
     reg = lc2_registration()
     reg.mode = MODES[mode]
     n = 6 if mode == "2D" else 12
@@ -483,7 +564,6 @@ def register(ctx, initial, lower, upper, center, shift=(0.0, 0.0, 0.0), direct_e
         reg.round_xtol[r] = float(xtol)
     reg.round_maxeval = int(round_maxeval)
     reg.local_algorithm = ALGORITHMS[local_algorithm]
-    err = []
     if lc2_of_matrices is not None:
         def cb(user, count, dim, xp, fp):
             try:
@@ -493,7 +573,9 @@ def register(ctx, initial, lower, upper, center, shift=(0.0, 0.0, 0.0), direct_e
             except Exception as e:
                 err.append(e)
                 return 1
-        reg.lc2_of_matrices = BATCH_OBJECTIVE(cb)
+        fn = BATCH_OBJECTIVE(cb)
+        keep.append(fn)  # the struct holds only the function pointer
+        reg.lc2_of_matrices = fn
     if observer is not None:
         def ob(user, stage, count, nparams, pp, lp):
             try:
@@ -502,15 +584,9 @@ def register(ctx, initial, lower, upper, center, shift=(0.0, 0.0, 0.0), direct_e
             except Exception as e:  # an observer cannot fail the C driver
                 err.append(e)
         ob_c = OBSERVER(ob)
+        keep.append(ob_c)
         reg.observer = ctypes.cast(ob_c, ctypes.c_void_p)
-    out = lc2_registration_result()
-    st = lib.lc2_register(ctx.handle if ctx is not None else None, ctypes.byref(reg),
-                          ctypes.byref(out))
-    if err:
-        raise err[0]
-    _check(st)
-    return dict(params=np.array(out.params[:n]), lc2=out.lc2, evaluations=out.evaluations,
-                launches=out.launches)
+    return reg
 
 
 def params_to_matrix(mode: str, params, center, shift=(0.0, 0.0, 0.0)) -> np.ndarray:
@@ -526,3 +602,83 @@ def params_to_matrix(mode: str, params, center, shift=(0.0, 0.0, 0.0)) -> np.nda
     _check(lib.lc2_params_to_matrix(MODES[mode], p.ctypes.data_as(_dp), c.ctypes.data_as(_fp),
                                     sh.ctypes.data_as(_fp), m.ctypes.data_as(_fp)))
     return m.reshape(3, 3) if mode == "2D" else m.reshape(4, 4)
+
+
+class Server:
+    """lc2_server_*: registrations admitted by device-memory budget, run
+    concurrently on worker threads, results polled by ticket."""
+
+    def __init__(self, budget_bytes: int = 0, max_active: int = 0, device: int = 0):
+        lib = load()
+        self._lib = lib
+        self._h = ctypes.c_void_p()
+        cfg = lc2_server_config(int(budget_bytes), int(max_active), int(device))
+        _check(lib.lc2_server_create(ctypes.byref(cfg), ctypes.byref(self._h)))
+        self._keep = {}   # ticket -> callback objects the C side may still call
+        self._errs = {}
+
+    def close(self):
+        if self._h:
+            self._lib.lc2_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, cfg: lc2_config, fixed=None, moving=None, **registration) -> int:
+        """Queues one registration; registration holds make_registration's
+        arguments (initial, lower, upper, center, ...; mode is taken from cfg)."""
+        mode = {v: k for k, v in MODES.items()}[cfg.mode]
+        err, keep = [], []
+        reg = make_registration(mode, err=err, keep=keep, **registration)
+        req = lc2_request()
+        req.config = cfg
+        imgs = []
+        if fixed is not None:
+            f, m = _f32(fixed), _f32(moving)
+            imgs = [f, m]
+            req.fixed = f.ctypes.data_as(_fp)
+            req.moving = m.ctypes.data_as(_fp)
+        req.registration = reg
+        t = ctypes.c_longlong()
+        _check(self._lib.lc2_server_submit(self._h, ctypes.byref(req), ctypes.byref(t)))
+        del imgs  # copied by the server
+        self._keep[t.value] = keep
+        self._errs[t.value] = err
+        return t.value
+
+    def poll(self, ticket: int, wait_ms: int = -1):
+        """The result dict, or None while the request is queued or running."""
+        out = lc2_request_result()
+        st = self._lib.lc2_server_poll(self._h, int(ticket), int(wait_ms), ctypes.byref(out))
+        if st == 4:
+            return None
+        _check(st)
+        self._keep.pop(ticket, None)
+        err = self._errs.pop(ticket, [])
+        if err:
+            raise err[0]
+        r = out.result
+        return dict(status=out.status, message=out.message.decode(), params=np.array(r.params[:]),
+                    lc2=r.lc2, evaluations=r.evaluations, launches=r.launches,
+                    queue_ms=out.queue_ms, run_ms=out.run_ms, total_ms=out.total_ms,
+                    device_bytes=out.device_bytes, admission=out.admission)
+
+    def drain(self, wait_ms: int = -1) -> bool:
+        st = self._lib.lc2_server_drain(self._h, int(wait_ms))
+        if st == 4:
+            return False
+        _check(st)
+        return True
+
+    def stats(self) -> dict:
+        st = lc2_server_stats()
+        _check(self._lib.lc2_server_get_stats(self._h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in lc2_server_stats._fields_}
+
+    def reset_stats(self):
+        _check(self._lib.lc2_server_reset_stats(self._h))

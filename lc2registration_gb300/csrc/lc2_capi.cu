@@ -71,6 +71,7 @@ struct lc2_context {
   float* d_gstatic = nullptr;  // hr_fixed: Sobel(M)
   float* d_scratch = nullptr;  // per-slot warped image (+ Sobel when hr_moving)
   int slots = 1;
+  size_t per_slot = 0;  // scratch bytes per slot
   lc2::Xform* d_xf = nullptr;
   unsigned long long* d_acc = nullptr;
   double* d_out = nullptr;
@@ -442,9 +443,9 @@ const char* lc2_version(void) { return "lc2-gb300 0.1 (sm_103a)"; }
 
 namespace {
 
-int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
-  if (!cfg || !out) return fail(LC2_ERR_INVALID_ARGUMENT, "null config or output pointer");
-  *out = nullptr;
+// Host-side plan of a context: validation, virtual grid, sizes, patch and
+// fixed-point bits, scratch slots. No device work.
+int plan_context(const lc2_config* cfg, lc2_context* c) {
   if (cfg->mode < LC2_MODE_2D || cfg->mode > LC2_MODE_2DTO3D)
     return fail(LC2_ERR_INVALID_ARGUMENT, "unknown mode %d", cfg->mode);
   if (cfg->storage < LC2_STORE_F32 || cfg->storage > LC2_STORE_BF16)
@@ -455,8 +456,6 @@ int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
     if (!std::isfinite(cfg->virtual_spacing[a]) || !(cfg->virtual_spacing[a] > 0.0f))
       if (!(cfg->mode == LC2_MODE_2D && a == 2))
         return fail(LC2_ERR_INVALID_ARGUMENT, "virtual spacing must be finite and > 0");
-  lc2_context* c = new (std::nothrow) lc2_context();
-  if (!c) return fail(LC2_ERR_OUT_OF_MEMORY, "host allocation failed");
   c->cfg = *cfg;
   c->warp_nd = (cfg->mode == LC2_MODE_2D) ? 2 : 3;
   c->lc2_nd = (cfg->mode == LC2_MODE_3D) ? 3 : 2;
@@ -480,16 +479,12 @@ int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
   }
   int r = cfg->patch_size;
   int rmax = (c->lc2_nd == 3) ? 6 : 12;
-  if (r < 1 || r > rmax) {
-    delete c;
+  if (r < 1 || r > rmax)
     return fail(LC2_ERR_UNSUPPORTED, "patch size %d outside [1, %d] for %dD patches", r, rmax,
                 c->lc2_nd);
-  }
-  if (cfg->mode == LC2_MODE_2DTO3D && c->virt.dim[2] != 1) {
-    delete c;
+  if (cfg->mode == LC2_MODE_2DTO3D && c->virt.dim[2] != 1)
     return fail(LC2_ERR_INVALID_ARGUMENT,
                 "2D-to-3D needs a single virtual slice (fixed z extent <= virtual z spacing)");
-  }
   c->nv = (size_t)c->virt.dim[0] * c->virt.dim[1] * c->virt.dim[2];
   c->nf = (size_t)c->cfg.fixed.dim[0] * c->cfg.fixed.dim[1] * c->cfg.fixed.dim[2];
   c->nm = (size_t)c->cfg.moving.dim[0] * c->cfg.moving.dim[1] * c->cfg.moving.dim[2];
@@ -499,8 +494,43 @@ int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
   int b = 0;
   while (b < 21 && ((long long)c->n << (b + 2)) <= (1LL << 31)) ++b;
   c->qbits = b;
+  // scratch slots: warped image (+ its Sobel when the moving image is the
+  // high-resolution one). The fused path (static ultrasound) keeps nothing
+  // per transform and needs one slot; the generic path takes as many as fit
+  // 1 GiB unless max_batch says more.
+  c->per_slot = c->nv * sizeof(float) * (cfg->high_res_is_moving ? 2 : 1);
+  long long slots = cfg->max_batch > 0 ? cfg->max_batch
+                    : cfg->high_res_is_moving
+                        ? 1
+                        : std::max<long long>(1, (1LL << 30) / (long long)c->per_slot);
+  slots = std::min<long long>(slots, 1024);
+  slots = std::min<long long>(slots, 65535 / c->virt.dim[2]);
+  c->slots = (int)std::max<long long>(1, slots);
+  return LC2_OK;
+}
 
-  int st = select_device(c);
+// Device bytes a context of this plan holds, and the largest temporary
+// allocation of lc2_set_images on top of them.
+void context_bytes(const lc2_context* c, size_t* held, size_t* peak_extra) {
+  const size_t es = elem_size(c->cfg.storage);
+  const bool hrm = c->cfg.high_res_is_moving != 0;
+  size_t h = c->per_slot * c->slots;
+  h += c->nm * es;                             // moving
+  h += c->nv * (hrm ? es : sizeof(float));     // static image on the virtual grid
+  if (!hrm) h += c->nv * sizeof(float);        // its Sobel
+  if (hrm) h += c->nv * sizeof(float);         // weighting factors
+  h += 64 * (sizeof(lc2::Xform) + 2 * sizeof(unsigned long long) + sizeof(double));
+  *held = h;
+  *peak_extra = std::max(c->nm, c->nf) * sizeof(float);
+}
+
+int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
+  if (!cfg || !out) return fail(LC2_ERR_INVALID_ARGUMENT, "null config or output pointer");
+  *out = nullptr;
+  lc2_context* c = new (std::nothrow) lc2_context();
+  if (!c) return fail(LC2_ERR_OUT_OF_MEMORY, "host allocation failed");
+  int st = plan_context(cfg, c);
+  if (st == LC2_OK) st = select_device(c);
   if (st != LC2_OK) {
     delete c;
     return st;
@@ -511,15 +541,7 @@ int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
     return fail(LC2_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
   }
   c->stream = c->own_stream;
-  // scratch slots: warped image (+ its Sobel when the moving image is the
-  // high-resolution one), within a 1 GiB budget unless max_batch says more
-  size_t per_slot = c->nv * sizeof(float) * (cfg->high_res_is_moving ? 2 : 1);
-  long long slots = cfg->max_batch > 0 ? cfg->max_batch
-                                       : std::max<long long>(1, (1LL << 30) / (long long)per_slot);
-  slots = std::min<long long>(slots, 1024);
-  slots = std::min<long long>(slots, 65535 / c->virt.dim[2]);
-  c->slots = (int)std::max<long long>(1, slots);
-  e = cudaMalloc(&c->d_scratch, per_slot * c->slots);
+  e = cudaMalloc(&c->d_scratch, c->per_slot * c->slots);
   c->owns_moving = own_moving;
   if (e == cudaSuccess && own_moving) e = cudaMalloc(&c->d_moving, c->nm * elem_size(cfg->storage));
   if (e == cudaSuccess)
@@ -551,6 +573,17 @@ extern "C" {
 int lc2_create(const lc2_config* cfg, lc2_context** out) {
   g_err.clear();
   return create_context(cfg, true, out);
+}
+
+int lc2_context_bytes(const lc2_config* cfg, size_t* held, size_t* peak) {
+  g_err.clear();
+  if (!cfg || !held) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  lc2_context c;
+  LC2_TRY(plan_context(cfg, &c));
+  size_t extra = 0;
+  context_bytes(&c, held, &extra);
+  if (peak) *peak = *held + extra;
+  return LC2_OK;
 }
 
 int lc2_destroy(lc2_context* c) {

@@ -1,0 +1,62 @@
+"""The request loop on the GPU: a mixed stream of 2D, 3D and 2D-to-3D
+registrations submitted at random times runs concurrently (each on its own
+context and stream), and every result equals, bit for bit, the same
+registration run alone."""
+import time
+
+import numpy as np
+import pytest
+
+from lc2registration_gb300 import capi, synth
+from lc2registration_gb300.geometry import Geometry
+from tests.helpers import make_context
+
+pytestmark = pytest.mark.gpu
+
+
+def _reg(case):
+    c = case.fixed_geom.center()
+    if case.mode == "2D":
+        return dict(initial=[0, 0, 0, 1, 1, 0], lower=[-10, -10, -8, 0.9, 0.9, -0.06],
+                    upper=[10, 10, 8, 1.1, 1.1, 0.06], center=c, direct_entries=["translation"],
+                    direct_maxeval=40, rounds=[(["translation", "rotation"], 1e-4)])
+    lo = [-10, -10, -10, -8, -8, -8, 0.9, 0.9, 0.9, -0.05, -0.05, -0.05]
+    hi = [10, 10, 10, 8, 8, 8, 1.1, 1.1, 1.1, 0.05, 0.05, 0.05]
+    return dict(initial=[0, 0, 0, 0, 0, 0, 1, 1, 1, 0, 0, 0], lower=lo, upper=hi, center=c,
+                direct_entries=["translation"], direct_maxeval=40,
+                rounds=[(["translation", "rotation"], 1e-3)])
+
+
+def _mix():
+    cases = [synth.case_2d(seed=s, size=96, r=3) for s in (11, 12, 13)]
+    cases += [synth.case_3d(seed=s, mr_size=40, us_size=32, r=2, blobs=6) for s in (14, 15)]
+    mr = synth.mr_phantom((48, 48, 48), 8, 1.5, seed=16)
+    mg = Geometry((48, 48, 48), (1.0, 1.0, 1.0), (0.0, 0.0, 0.0))
+    cases += synth.frame_stack(mr, mg, 2, seed=17, sides=(40, 56), spacing=0.5, r=3)
+    return cases
+
+
+def test_mixed_stream_equals_alone():
+    cases = _mix()
+    alone = [capi.register(make_context(c), **_reg(c)) for c in cases]
+    srv = capi.Server(budget_bytes=2 << 30, max_active=4)
+    rng = np.random.default_rng(5)
+    tickets = []
+    for i in rng.permutation(len(cases)):
+        c = cases[i]
+        cfg = capi.make_config(c.mode, c.fixed_geom, c.moving_geom, c.virt_spacing, c.r,
+                               c.hr_moving)
+        tickets.append((i, srv.submit(cfg, c.fixed, c.moving, **_reg(c))))
+        time.sleep(rng.exponential(0.01))
+    for i, t in tickets:
+        r = srv.poll(t)
+        assert r["status"] == 0, r["message"]
+        n = 6 if cases[i].mode == "2D" else 12
+        np.testing.assert_array_equal(r["params"][:n], alone[i]["params"])
+        assert r["lc2"] == alone[i]["lc2"]
+        assert r["evaluations"] == alone[i]["evaluations"]
+    st = srv.stats()
+    assert st["completed"] == len(cases) and st["failed"] == 0
+    assert st["peak_active"] >= 2            # requests did overlap
+    assert st["p99_ms"] >= st["p50_ms"] > 0
+    srv.close()
