@@ -301,6 +301,7 @@ def main():
     ctx = capi.Context(case.mode, case.fixed_geom, case.moving_geom, case.virt_spacing, case.r,
                        case.hr_moving, args.storage, device=local)
     ctx.set_images(case.fixed, case.moving)
+    tuned = ctx.autotune(mats[:64])  # tile height and z-chunk, timed on 64 transforms
     K = mats.shape[0]
     stream = torch.cuda.ExternalStream(ctx.stream())
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")
@@ -410,7 +411,8 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic",
-            "config": config_dict(args, case),
+            "config": dict(config_dict(args, case), autotuned={"tile_rows": tuned[0],
+                                                                  "zchunk": tuned[1]}),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "k_fused", "kernel_ms_per_launch": mom_ms / max(1, mom_launches),

@@ -124,7 +124,24 @@ long long lc2_launch_count(const lc2_context* ctx);
  * automatic. No counterpart in the reference (its block sizes are arguments
  * of CalculateGradient / GetSimilarityMetric, src/cu_LC2/cu_lc2_3d.cuh:36-41). */
 enum { LC2_OPTION_TILE_ROWS = 1 };
+/* LC2_OPTION_ZCHUNK: output slices each CTA of the fused 3D kernel marches
+ * through (0 = automatic). LC2_OPTION_GRAPHS: 1 (default) replays
+ * lc2_evaluate_batch / lc2_evaluate from a CUDA graph captured once per batch
+ * size; 0 issues the calls one by one. None of the options changes a
+ * result: every sum is exact, whatever the tiling. */
+enum { LC2_OPTION_ZCHUNK = 2, LC2_OPTION_GRAPHS = 3 };
 int lc2_set_option(lc2_context* ctx, int option, int value);
+
+/* CUDA-graph launches issued by lc2_evaluate_batch / lc2_evaluate. */
+long long lc2_graph_launches(const lc2_context* ctx);
+
+/* Autotuner: times the fused kernel on `count` transforms (matrices as in
+ * lc2_evaluate_batch) for each tile height and z-chunk length it supports,
+ * keeps the fastest as the context's options and returns them. Contexts
+ * without a tunable kernel (2D windows, HighResolutionModality: Fixed)
+ * return their current settings. The reference takes fixed block sizes as
+ * arguments (src/cu_LC2/cu_lc2_3d.cuh:36-41). */
+int lc2_autotune(lc2_context* ctx, const float* matrices, int count, int* tile_rows, int* zchunk);
 
 /* Per-kernel device timing with CUDA events on the context stream (off by
  * default). lc2_kernel_times synchronises, returns the summed milliseconds

@@ -26,6 +26,8 @@ STATUS_NAMES = {
 }
 MODES = {"2D": 0, "3D": 1, "2DTo3D": 2}
 OPTION_TILE_ROWS = 1
+OPTION_ZCHUNK = 2
+OPTION_GRAPHS = 3
 STORAGE = {"f32": 0, "f16": 1, "bf16": 2}
 
 # Every symbol include/lc2.h declares (checked by the test suite).
@@ -41,6 +43,7 @@ EXPORTED = [
     "lc2_stack_launch_count", "lc2_stack_graph_launches", "lc2_context_bytes",
     "lc2_server_create", "lc2_server_submit", "lc2_server_poll", "lc2_server_drain",
     "lc2_server_get_stats", "lc2_server_reset_stats", "lc2_server_destroy",
+    "lc2_graph_launches", "lc2_autotune",
 ]
 
 ALGORITHMS = {"direct_l": 1, "bobyqa": 2, "nelder_mead": 3}
@@ -198,6 +201,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "lc2_server_get_stats": ([vp, ctypes.POINTER(lc2_server_stats)], ctypes.c_int),
         "lc2_server_reset_stats": ([vp], ctypes.c_int),
         "lc2_server_destroy": ([vp], ctypes.c_int),
+        "lc2_graph_launches": ([vp], ctypes.c_longlong),
+        "lc2_autotune": ([vp, _fp, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                          ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -336,6 +342,18 @@ class Context:
 
     def set_option(self, option: int, value: int):
         _check(self._lib.lc2_set_option(self._h, int(option), int(value)))
+
+    def graph_launches(self) -> int:
+        return int(self._lib.lc2_graph_launches(self._h))
+
+    def autotune(self, mats):
+        """Times the fused kernel's tilings on these transforms, keeps the
+        fastest; returns (tile_rows, zchunk)."""
+        m = self._mats(mats)
+        tr, zc = ctypes.c_int(), ctypes.c_int()
+        _check(self._lib.lc2_autotune(self._h, m.ctypes.data_as(_fp), m.shape[0],
+                                      ctypes.byref(tr), ctypes.byref(zc)))
+        return tr.value, zc.value
 
     def enable_kernel_timing(self, on: bool = True):
         _check(self._lib.lc2_enable_kernel_timing(self._h, int(bool(on))))

@@ -88,6 +88,18 @@ struct lc2_context {
   float* d_sigma = nullptr;
   long long sigma_sum = -1;
   int tile_rows = 0;  // fused kernel tile height (0 = automatic)
+  int zchunk = 0;     // fused kernel output slices per CTA (0 = automatic)
+
+  // CUDA graphs of lc2_evaluate_batch's sequence (copy-in, fused launch,
+  // ratio, copy-out) by batch size; dropped when buffers or options change
+  struct Graph {
+    int count;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+  };
+  std::vector<Graph> graphs;
+  bool use_graphs = true;
+  long long graph_launches = 0;
 
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
@@ -199,8 +211,17 @@ long long floor_clamp(long double v) {
   return (long long)std::floor(v);
 }
 
+void drop_graphs(lc2_context* c) {
+  for (auto& g : c->graphs) {
+    cudaGraphExecDestroy(g.exec);
+    cudaGraphDestroy(g.graph);
+  }
+  c->graphs.clear();
+}
+
 int ensure_capacity(lc2_context* c, int count) {
   if (count <= c->cap) return LC2_OK;
+  drop_graphs(c);  // the graphs read the buffers being replaced
   int ncap = std::max(count, std::max(64, c->cap * 2));
   if (c->d_xf) cudaFree(c->d_xf);
   if (c->d_acc) cudaFree(c->d_acc);
@@ -393,6 +414,7 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
   L.nd = c->lc2_nd;
   L.wnd = c->warp_nd;
   L.tile_height = c->tile_rows > 0 ? c->tile_rows : 16;
+  L.zchunk = c->zchunk;
   L.stream = c->stream;
   cudaError_t e;
   {
@@ -595,6 +617,7 @@ int lc2_destroy(lc2_context* c) {
   cudaFree(c->d_gstatic);
   cudaFree(c->d_sigma);
   cudaFree(c->d_scratch);
+  drop_graphs(c);
   cudaFree(c->d_xf);
   cudaFree(c->d_acc);
   cudaFree(c->d_out);
@@ -630,7 +653,21 @@ int lc2_set_option(lc2_context* c, int option, int value) {
   if (option == LC2_OPTION_TILE_ROWS) {
     if (value != 0 && value != 8 && value != 16)
       return fail(LC2_ERR_INVALID_ARGUMENT, "tile rows must be 0, 8 or 16");
+    if (value == 16 && c->lc2_nd == 3 && c->cfg.patch_size > 4)
+      return fail(LC2_ERR_UNSUPPORTED, "16-row tiles need a 3D patch radius <= 4");
     c->tile_rows = value;
+    drop_graphs(c);
+    return LC2_OK;
+  }
+  if (option == LC2_OPTION_ZCHUNK) {
+    if (value < 0) return fail(LC2_ERR_INVALID_ARGUMENT, "z chunk must be >= 0");
+    c->zchunk = value;
+    drop_graphs(c);
+    return LC2_OK;
+  }
+  if (option == LC2_OPTION_GRAPHS) {
+    c->use_graphs = value != 0;
+    if (!c->use_graphs) drop_graphs(c);
     return LC2_OK;
   }
   return fail(LC2_ERR_INVALID_ARGUMENT, "unknown option %d", option);
@@ -813,11 +850,14 @@ int lc2_set_images(lc2_context* c, const float* fixed, const float* moving) {
   return set_fixed(c, fixed, fmax, mmax);
 }
 
-int lc2_stage_transforms(lc2_context* c, const float* matrices, int count) {
-  g_err.clear();
-  LC2_TRY(check_ctx(c));
+}  // extern "C"
+
+namespace {
+
+// Validates the matrices and writes their per-transform affines into the
+// pinned staging buffer (no device work).
+int stage_host(lc2_context* c, const float* matrices, int count) {
   if (count < 0 || (count > 0 && !matrices)) return fail(LC2_ERR_INVALID_ARGUMENT, "bad transforms");
-  LC2_TRY(select_device(c));
   LC2_TRY(ensure_capacity(c, count));
   const int mf = matrix_floats(c);
   for (int k = 0; k < count; ++k) {
@@ -826,6 +866,67 @@ int lc2_stage_transforms(lc2_context* c, const float* matrices, int count) {
       if (!std::isfinite(m[i])) return fail(LC2_ERR_INVALID_ARGUMENT, "transform %d has NaN/Inf", k);
     build_xform(c->warp_nd, c->virt, c->cfg.moving, m, &c->h_xf[k]);
   }
+  return LC2_OK;
+}
+
+// lc2_evaluate_batch's device sequence for a static-ultrasound context.
+int enqueue_batch(lc2_context* c, int count) {
+  LC2_CUDA(cudaMemcpyAsync(c->d_xf, c->h_xf, sizeof(lc2::Xform) * count, cudaMemcpyHostToDevice,
+                           c->stream));
+  LC2_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2 * count, c->stream));
+  LC2_TRY(launch_fused(c, 0, count, nullptr));
+  LC2_TRY(launch_finalize(c, count));
+  LC2_CUDA(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(double) * count, cudaMemcpyDeviceToHost,
+                           c->stream));
+  return LC2_OK;
+}
+
+// The same sequence through a CUDA graph captured once per batch size.
+int launch_batch_graph(lc2_context* c, int count) {
+  lc2_context::Graph* g = nullptr;
+  for (auto& cand : c->graphs)
+    if (cand.count == count) g = &cand;
+  if (!g) {
+    if (c->graphs.size() >= 16) {
+      cudaGraphExecDestroy(c->graphs.front().exec);
+      cudaGraphDestroy(c->graphs.front().graph);
+      c->graphs.erase(c->graphs.begin());
+    }
+    LC2_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+    const long long before = c->launches;
+    int st = enqueue_batch(c, count);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    c->launches = before;  // counted when the graph runs
+    if (st != LC2_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return st;
+    }
+    LC2_CUDA(e);
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      LC2_CUDA(e);
+    }
+    c->graphs.push_back({count, graph, exec});
+    g = &c->graphs.back();
+  }
+  LC2_CUDA(cudaGraphLaunch(g->exec, c->stream));
+  c->launches += 2;  // fused kernel and ratio
+  ++c->graph_launches;
+  return LC2_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lc2_stage_transforms(lc2_context* c, const float* matrices, int count) {
+  g_err.clear();
+  LC2_TRY(check_ctx(c));
+  LC2_TRY(select_device(c));
+  LC2_TRY(stage_host(c, matrices, count));
   if (count > 0)
     LC2_CUDA(cudaMemcpyAsync(c->d_xf, c->h_xf, sizeof(lc2::Xform) * count, cudaMemcpyHostToDevice,
                              c->stream));
@@ -864,10 +965,24 @@ int lc2_fetch_results(lc2_context* c, double* out, int count) {
 }
 
 int lc2_evaluate_batch(lc2_context* c, const float* matrices, int count, double* out) {
+  g_err.clear();
+  LC2_TRY(check_ctx(c));
+  if (count > 0 && !out) return fail(LC2_ERR_INVALID_ARGUMENT, "null output");
+  if (c->cfg.high_res_is_moving && c->use_graphs && !c->timing && count > 0) {
+    LC2_TRY(select_device(c));
+    LC2_TRY(stage_host(c, matrices, count));
+    c->staged = count;
+    LC2_TRY(launch_batch_graph(c, count));
+    LC2_CUDA(cudaStreamSynchronize(c->stream));
+    std::memcpy(out, c->h_out, sizeof(double) * count);
+    return LC2_OK;
+  }
   LC2_TRY(lc2_stage_transforms(c, matrices, count));
   LC2_TRY(lc2_launch_staged(c, count));
   return lc2_fetch_results(c, out, count);
 }
+
+long long lc2_graph_launches(const lc2_context* c) { return c ? c->graph_launches : 0; }
 
 int lc2_evaluate(lc2_context* c, const float* matrix, double* out) {
   if (!out) return fail(LC2_ERR_INVALID_ARGUMENT, "null output");
@@ -1383,3 +1498,71 @@ int lc2_stack_evaluate(lc2_stack* s, int count, const int* frame_ids, const floa
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Autotuner
+// ---------------------------------------------------------------------------
+
+extern "C" int lc2_autotune(lc2_context* c, const float* matrices, int count, int* tile_rows,
+                            int* zchunk) {
+  g_err.clear();
+  LC2_TRY(check_ctx(c));
+  if (count < 1) return fail(LC2_ERR_INVALID_ARGUMENT, "autotune needs at least one transform");
+  LC2_TRY(select_device(c));
+  const int r = c->cfg.patch_size;
+  if (c->lc2_nd == 3 && c->cfg.high_res_is_moving) {
+    LC2_TRY(lc2_stage_transforms(c, matrices, count));
+    std::vector<int> rows = (r <= 4) ? std::vector<int>{16, 8} : std::vector<int>{8};
+    const int vz = c->virt.dim[2];
+    std::vector<int> chunks{0};
+    for (int zc : {vz, vz / 2, vz / 4, 64, 32})
+      if (zc >= 2 * r + 2 && zc <= vz && std::find(chunks.begin(), chunks.end(), zc) == chunks.end())
+        chunks.push_back(zc);
+    cudaEvent_t a = nullptr, b = nullptr;
+    LC2_CUDA(cudaEventCreate(&a));
+    struct Ev {
+      cudaEvent_t& e;
+      ~Ev() { if (e) cudaEventDestroy(e); }
+    } ga{a}, gb{b};
+    LC2_CUDA(cudaEventCreate(&b));
+    const bool timing = c->timing;
+    c->timing = false;
+    float best = 0.0f;
+    int best_rows = rows[0], best_chunk = 0;
+    int st = LC2_OK;
+    for (int tr : rows) {
+      for (int zc : chunks) {
+        c->tile_rows = tr;
+        c->zchunk = zc;
+        float ms = 0.0f;
+        for (int rep = 0; rep < 2 && st == LC2_OK; ++rep) {  // warm-up, then timed
+          if (cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2 * count, c->stream) != cudaSuccess ||
+              cudaEventRecord(a, c->stream) != cudaSuccess) {
+            st = fail(LC2_ERR_CUDA, "autotune: %s", cudaGetErrorString(cudaGetLastError()));
+            break;
+          }
+          st = launch_fused(c, 0, count, nullptr);
+          if (st == LC2_OK && (cudaEventRecord(b, c->stream) != cudaSuccess ||
+                               cudaEventSynchronize(b) != cudaSuccess ||
+                               cudaEventElapsedTime(&ms, a, b) != cudaSuccess))
+            st = fail(LC2_ERR_CUDA, "autotune timing: %s", cudaGetErrorString(cudaGetLastError()));
+        }
+        if (st != LC2_OK) break;
+        if (best == 0.0f || ms < best) {
+          best = ms;
+          best_rows = tr;
+          best_chunk = zc;
+        }
+      }
+      if (st != LC2_OK) break;
+    }
+    c->timing = timing;
+    c->tile_rows = best_rows;
+    c->zchunk = best_chunk;
+    drop_graphs(c);
+    if (st != LC2_OK) return st;
+  }
+  if (tile_rows) *tile_rows = c->tile_rows > 0 ? c->tile_rows : 16;
+  if (zchunk) *zchunk = c->zchunk;
+  return LC2_OK;
+}

@@ -344,11 +344,16 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
   const int x0 = (tile % P.ntx) * 32, y0 = (tile / P.ntx) * TY;
   const Xform* X = xf + k0 + slot;
   const int gx0 = x0 - R - 1, gy0 = y0 - R - 1;  // origin of the resampled region
+  // Sampling base: (x0 - R - 1, 16 floor(y0 / 16) - R - 1). Tiles are 32
+  // wide in every kernel and 8 or 16 rows high, so this base -- and with it
+  // every sample, patch sum and LC2 value -- is the same whichever tile
+  // height computes an output voxel. yb: row offset of the region origin.
+  const int yb = y0 & 15;
   const int ox = tid & 31, oy = tid >> 5;
   long long acc_m = 0;
 
-  // thread 0: base coordinate of the region at slice zs in double, split into
-  // integer part and fraction for the float per-point offsets
+  // thread 0: sampling base at slice zs in double, split into integer part
+  // and fraction for the float per-point offsets
   auto set_base = [&](int zs) {
     if (tid == 0) {
 #pragma unroll
@@ -363,7 +368,7 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
   if (tid == 0) {
 #pragma unroll
     for (int a = 0; a < 3; ++a)
-      s_base[a] = X->A[3 * a + 0] * gx0 + X->A[3 * a + 1] * gy0 + X->b[a];
+      s_base[a] = X->A[3 * a + 0] * gx0 + X->A[3 * a + 1] * (gy0 - yb) + X->b[a];
 #pragma unroll
     for (int i = 0; i < 9; ++i) s_A[i] = (float)X->A[i];
   }
@@ -444,7 +449,7 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
           const int py = i / G::PW, px = i - py * G::PW;
           const int gx = gx0 + px, gy = gy0 + py;
           if (zin && gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy)
-            v = fused_sample<3, TM>(mov, P, s_A, s_ib, s_fb, px, py);
+            v = fused_sample<3, TM>(mov, P, s_A, s_ib, s_fb, px, py + yb);
         }
         out[k] = v;
       }
@@ -537,6 +542,7 @@ struct FusedLaunch {
   float* out_measure;
   int nd, wnd;
   int tile_height;  // 3D, radius <= 4: 16 or 8 rows per tile
+  int zchunk;       // 3D: output slices per CTA; 0 = automatic
   cudaStream_t stream;
 };
 
@@ -551,7 +557,10 @@ cudaError_t fused_launch_rt(const FusedLaunch& L) {
   const int ntx = (P.vx + 31) / 32, nty = (P.vy + TY - 1) / TY;
   P.ntx = ntx;
   int nz = 1;
-  if (ND == 3) {
+  if (ND == 3 && L.zchunk > 0) {
+    P.zchunk = L.zchunk < P.vz ? L.zchunk : P.vz;
+    nz = (P.vz + P.zchunk - 1) / P.zchunk;
+  } else if (ND == 3) {
     const long long ctas = (long long)ntx * nty * L.cnt;
     nz = (int)((4LL * 152 + ctas - 1) / ctas);
     nz = nz < 1 ? 1 : nz;
