@@ -55,7 +55,8 @@ typedef struct {
     lc2_geometry fixed;      /* FixedImage / FixedVolume */
     lc2_geometry moving;     /* MovingImage / MovingVolume */
     float virtual_spacing[3];/* RegistrationParameters.ResampledSpacing */
-    int patch_size;          /* RegistrationParameters.PatchSize (radius r, patch 2r+1) */
+    int patch_size;          /* RegistrationParameters.PatchSize (radius r, patch 2r+1);
+                              * 0 = normalised mutual information (3D) */
     int high_res_is_moving;  /* HighResolutionModality: 1 = Moving, 0 = Fixed */
     int storage;             /* lc2_storage */
     int max_batch;           /* transforms per launch group; 0 = automatic */
@@ -79,6 +80,9 @@ int lc2_destroy(lc2_context* ctx);
  * static virtual-grid image. Replaces the FixedVolume_d / MovingVolume_d
  * uploads (src/Interpolator/interpolator.cu:276,315,459-473). */
 int lc2_set_images(lc2_context* ctx, const float* fixed_host, const float* moving_host);
+
+/* The configuration the context was created with. */
+int lc2_get_config(const lc2_context* ctx, lc2_config* out);
 
 /* Virtual grid dims (src/Interpolator/interpolator.cu:337-339). */
 int lc2_virtual_dims(const lc2_context* ctx, int dims[3]);
@@ -233,6 +237,10 @@ typedef struct {
     void (*observer)(void* user, int stage, int count, int nparams, const double* params,
                      const double* lc2);
     void* observer_user;
+    /* 1: the similarity is maximised as it is (normalised mutual information,
+     * src/Optimizers/optimizers.cu:722-724, 855-860); 0: -log(LC2) is
+     * minimised. Set automatically for a context with patch_size 0. */
+    int maximize;
 } lc2_registration;
 typedef struct {
     double params[12];     /* optimum, reference order */

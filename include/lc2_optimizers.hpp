@@ -38,7 +38,8 @@ class OptimizersBase {
 
   void LinkToInterpolator(Interp* external_Interpolator) { interp_ = external_Interpolator; }
 
-  // objective of the reference: -log(LC2) at x for the entries being optimised
+  // objective of the reference: -log(LC2) at x for the entries being optimised,
+  // or the NMI itself for PatchSize 0 (optimizers.cu:722-727)
   double operator()(const std::vector<double>& x) {
     std::vector<double> p = OptimalSolution;
     std::vector<int> idx = indices(current_mask_);
@@ -50,7 +51,7 @@ class OptimizersBase {
     check(lc2_evaluate(interp_->Handle(), m.data(), &v), "lc2_evaluate");
     SimilarityMeasure = v;
     ++EvalCounter;
-    return -std::log(v);
+    return interp_->PatchSize() == 0 ? v : -std::log(v);
   }
   static double wrapper(const std::vector<double>& x, std::vector<double>& grad, void* data) {
     (void)grad;

@@ -43,7 +43,7 @@ EXPORTED = [
     "lc2_stack_launch_count", "lc2_stack_graph_launches", "lc2_context_bytes",
     "lc2_server_create", "lc2_server_submit", "lc2_server_poll", "lc2_server_drain",
     "lc2_server_get_stats", "lc2_server_reset_stats", "lc2_server_destroy",
-    "lc2_graph_launches", "lc2_autotune",
+    "lc2_graph_launches", "lc2_autotune", "lc2_get_config",
 ]
 
 ALGORITHMS = {"direct_l": 1, "bobyqa": 2, "nelder_mead": 3}
@@ -76,7 +76,7 @@ class lc2_registration(ctypes.Structure):
                 ("round_xtol", ctypes.c_double * 8), ("round_maxeval", ctypes.c_int),
                 ("local_algorithm", ctypes.c_int), ("lc2_of_matrices", BATCH_OBJECTIVE),
                 ("user", ctypes.c_void_p), ("observer", ctypes.c_void_p),
-                ("observer_user", ctypes.c_void_p)]
+                ("observer_user", ctypes.c_void_p), ("maximize", ctypes.c_int)]
 
 
 class lc2_registration_result(ctypes.Structure):
@@ -202,6 +202,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "lc2_server_reset_stats": ([vp], ctypes.c_int),
         "lc2_server_destroy": ([vp], ctypes.c_int),
         "lc2_graph_launches": ([vp], ctypes.c_longlong),
+        "lc2_get_config": ([vp, ctypes.POINTER(lc2_config)], ctypes.c_int),
         "lc2_autotune": ([vp, _fp, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                           ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
     }
@@ -528,7 +529,7 @@ def _mask(entries) -> int:
 def register(ctx, initial, lower, upper, center, shift=(0.0, 0.0, 0.0), direct_entries=(),
              direct_maxeval: int = 50, rounds=(), round_maxeval: int = 0,
              local_algorithm: str = "bobyqa", mode: Optional[str] = None, lc2_of_matrices=None,
-             observer=None):
+             observer=None, maximize: bool = False):
     """lc2_register: DIRECT on direct_entries, then local rounds [(entries, xtol), ...].
 
     ctx: a Context (GPU objective) or None together with lc2_of_matrices, a
@@ -542,7 +543,7 @@ def register(ctx, initial, lower, upper, center, shift=(0.0, 0.0, 0.0), direct_e
     keep = []
     reg = make_registration(mode, initial, lower, upper, center, shift, direct_entries,
                             direct_maxeval, rounds, round_maxeval, local_algorithm,
-                            lc2_of_matrices, observer, err, keep)
+                            lc2_of_matrices, observer, err, keep, maximize)
     out = lc2_registration_result()
     st = lib.lc2_register(ctx.handle if ctx is not None else None, ctypes.byref(reg),
                           ctypes.byref(out))
@@ -557,7 +558,8 @@ def register(ctx, initial, lower, upper, center, shift=(0.0, 0.0, 0.0), direct_e
 def make_registration(mode, initial, lower, upper, center, shift=(0.0, 0.0, 0.0),
                       direct_entries=(), direct_maxeval: int = 50, rounds=(),
                       round_maxeval: int = 0, local_algorithm: str = "bobyqa",
-                      lc2_of_matrices=None, observer=None, err=None, keep=None):
+                      lc2_of_matrices=None, observer=None, err=None, keep=None,
+                      maximize: bool = False):
     """An lc2_registration struct. Python callbacks append their exceptions to
     err; the ctypes callback objects are appended to keep, which the caller
     holds while the struct is in use."""
@@ -582,6 +584,7 @@ def make_registration(mode, initial, lower, upper, center, shift=(0.0, 0.0, 0.0)
         reg.round_xtol[r] = float(xtol)
     reg.round_maxeval = int(round_maxeval)
     reg.local_algorithm = ALGORITHMS[local_algorithm]
+    reg.maximize = int(bool(maximize))
     if lc2_of_matrices is not None:
         def cb(user, count, dim, xp, fp):
             try:

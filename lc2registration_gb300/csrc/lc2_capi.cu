@@ -15,6 +15,7 @@
 #include "lc2_kernels.cuh"
 #include "lc2_fused.cuh"
 #include "lc2_list.cuh"
+#include "lc2_mi.cuh"
 
 namespace {
 
@@ -87,6 +88,14 @@ struct lc2_context {
   // voxel and its exact fixed-point sum
   float* d_sigma = nullptr;
   long long sigma_sum = -1;
+  // normalised mutual information (patch_size 0): static image bins and
+  // entropy, per-transform range and joint histogram
+  bool mi = false;
+  unsigned char* d_sbin = nullptr;
+  unsigned* d_hist = nullptr;
+  unsigned* d_rmin = nullptr;
+  unsigned* d_rmax = nullptr;
+  double h_static = 0.0;
   int tile_rows = 0;  // fused kernel tile height (0 = automatic)
   int zchunk = 0;     // fused kernel output slices per CTA (0 = automatic)
 
@@ -235,6 +244,15 @@ int ensure_capacity(lc2_context* c, int count) {
   LC2_CUDA(cudaMalloc(&c->d_out, sizeof(double) * ncap));
   LC2_CUDA(cudaMallocHost(&c->h_xf, sizeof(lc2::Xform) * ncap));
   LC2_CUDA(cudaMallocHost(&c->h_out, sizeof(double) * ncap));
+  if (c->mi) {
+    cudaFree(c->d_hist);
+    cudaFree(c->d_rmin);
+    cudaFree(c->d_rmax);
+    c->d_hist = nullptr; c->d_rmin = nullptr; c->d_rmax = nullptr;
+    LC2_CUDA(cudaMalloc(&c->d_hist, sizeof(unsigned) * lc2::kMiHist * (size_t)ncap));
+    LC2_CUDA(cudaMalloc(&c->d_rmin, sizeof(unsigned) * ncap));
+    LC2_CUDA(cudaMalloc(&c->d_rmax, sizeof(unsigned) * ncap));
+  }
   c->cap = ncap;
   return LC2_OK;
 }
@@ -431,6 +449,49 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
   return LC2_OK;
 }
 
+// Normalised mutual information of staged transforms [0, cnt): range,
+// joint histogram, entropies; results straight into d_out.
+int launch_mi(lc2_context* c, int cnt) {
+  const lc2_geometry& v = c->virt;
+  lc2::MiParams P;
+  P.mx = c->cfg.moving.dim[0];
+  P.my = c->cfg.moving.dim[1];
+  P.mz = c->cfg.moving.dim[2];
+  P.vx = v.dim[0];
+  P.vy = v.dim[1];
+  P.vz = v.dim[2];
+  P.warped_is_high_res = c->cfg.high_res_is_moving;
+  LC2_CUDA(cudaMemsetAsync(c->d_rmin, 0xff, sizeof(unsigned) * cnt, c->stream));
+  LC2_CUDA(cudaMemsetAsync(c->d_rmax, 0x00, sizeof(unsigned) * cnt, c->stream));
+  LC2_CUDA(cudaMemsetAsync(c->d_hist, 0, sizeof(unsigned) * lc2::kMiHist * (size_t)cnt, c->stream));
+  dim3 block(32, 8, 1);
+  // one launch covers at most 65535 / vz transforms (grid z limit)
+  const int per = std::max(1, 65535 / v.dim[2]);
+  for (int k0 = 0; k0 < cnt; k0 += per) {
+    const int n = std::min(per, cnt - k0);
+    dim3 grid((v.dim[0] + 31) / 32, (v.dim[1] + 7) / 8, v.dim[2] * n);
+    TimerScope ts(c, K_MOMENTS);
+    const int st = c->cfg.storage;
+    if (st == LC2_STORE_F16) {
+      lc2::k_mi_range<__half><<<grid, block, 0, c->stream>>>((const __half*)c->d_moving, P, c->d_xf, k0, c->d_rmin, c->d_rmax);
+      lc2::k_mi_hist<__half><<<grid, block, 0, c->stream>>>((const __half*)c->d_moving, P, c->d_xf, k0, c->d_sbin, c->d_rmin, c->d_rmax, c->d_hist);
+    } else if (st == LC2_STORE_BF16) {
+      lc2::k_mi_range<__nv_bfloat16><<<grid, block, 0, c->stream>>>((const __nv_bfloat16*)c->d_moving, P, c->d_xf, k0, c->d_rmin, c->d_rmax);
+      lc2::k_mi_hist<__nv_bfloat16><<<grid, block, 0, c->stream>>>((const __nv_bfloat16*)c->d_moving, P, c->d_xf, k0, c->d_sbin, c->d_rmin, c->d_rmax, c->d_hist);
+    } else {
+      lc2::k_mi_range<float><<<grid, block, 0, c->stream>>>((const float*)c->d_moving, P, c->d_xf, k0, c->d_rmin, c->d_rmax);
+      lc2::k_mi_hist<float><<<grid, block, 0, c->stream>>>((const float*)c->d_moving, P, c->d_xf, k0, c->d_sbin, c->d_rmin, c->d_rmax, c->d_hist);
+    }
+    c->launches += 2;
+    LC2_CUDA(cudaGetLastError());
+  }
+  lc2::k_mi_nmi<<<cnt, 1024, 0, c->stream>>>(c->d_hist, 0, P.warped_is_high_res, c->h_static,
+                                              (double)c->nv, c->d_out);
+  ++c->launches;
+  LC2_CUDA(cudaGetLastError());
+  return LC2_OK;
+}
+
 // Enqueue the evaluation of staged transforms [k0, k0 + cnt).
 int launch_group(lc2_context* c, int k0, int cnt) {
   if (c->cfg.high_res_is_moving) return launch_fused(c, k0, cnt, nullptr);
@@ -501,7 +562,11 @@ int plan_context(const lc2_config* cfg, lc2_context* c) {
   }
   int r = cfg->patch_size;
   int rmax = (c->lc2_nd == 3) ? 6 : 12;
-  if (r < 1 || r > rmax)
+  c->mi = (r == 0);
+  if (c->mi && cfg->mode != LC2_MODE_3D)
+    return fail(LC2_ERR_UNSUPPORTED,
+                "PatchSize 0 (normalised mutual information) is a 3D similarity");
+  if (!c->mi && (r < 1 || r > rmax))
     return fail(LC2_ERR_UNSUPPORTED, "patch size %d outside [1, %d] for %dD patches", r, rmax,
                 c->lc2_nd);
   if (cfg->mode == LC2_MODE_2DTO3D && c->virt.dim[2] != 1)
@@ -540,7 +605,8 @@ void context_bytes(const lc2_context* c, size_t* held, size_t* peak_extra) {
   h += c->nm * es;                             // moving
   h += c->nv * (hrm ? es : sizeof(float));     // static image on the virtual grid
   if (!hrm) h += c->nv * sizeof(float);        // its Sobel
-  if (hrm) h += c->nv * sizeof(float);         // weighting factors
+  if (hrm && !c->mi) h += c->nv * sizeof(float);  // weighting factors
+  if (c->mi) h += c->nv + 64 * (sizeof(unsigned) * (lc2::kMiHist + 2));
   h += 64 * (sizeof(lc2::Xform) + 2 * sizeof(unsigned long long) + sizeof(double));
   *held = h;
   *peak_extra = std::max(c->nm, c->nf) * sizeof(float);
@@ -571,8 +637,9 @@ int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
                    c->nv * (cfg->high_res_is_moving ? elem_size(cfg->storage) : sizeof(float)));
   if (e == cudaSuccess && !cfg->high_res_is_moving)
     e = cudaMalloc(&c->d_gstatic, c->nv * sizeof(float));
-  if (e == cudaSuccess && cfg->high_res_is_moving)
+  if (e == cudaSuccess && cfg->high_res_is_moving && !c->mi)
     e = cudaMalloc(&c->d_sigma, c->nv * sizeof(float));
+  if (e == cudaSuccess && c->mi) e = cudaMalloc(&c->d_sbin, c->nv);
   if (e != cudaSuccess) {
     lc2_destroy(c);
     return fail(LC2_ERR_OUT_OF_MEMORY, "device allocation: %s", cudaGetErrorString(e));
@@ -618,6 +685,10 @@ int lc2_destroy(lc2_context* c) {
   cudaFree(c->d_sigma);
   cudaFree(c->d_scratch);
   drop_graphs(c);
+  cudaFree(c->d_sbin);
+  cudaFree(c->d_hist);
+  cudaFree(c->d_rmin);
+  cudaFree(c->d_rmax);
   cudaFree(c->d_xf);
   cudaFree(c->d_acc);
   cudaFree(c->d_out);
@@ -629,6 +700,12 @@ int lc2_destroy(lc2_context* c) {
   }
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
+  return LC2_OK;
+}
+
+int lc2_get_config(const lc2_context* c, lc2_config* out) {
+  if (!c || !out) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  *out = c->cfg;
   return LC2_OK;
 }
 
@@ -733,6 +810,42 @@ int upload_image(lc2_context* c, const float* host, size_t n, void* dst, int sto
 // largest |value| (its scale enters the fixed-point parameters): the fixed
 // image on the virtual grid, the fixed-point parameters and, for a static
 // ultrasound, the weighting factors and their sum.
+// Normalised mutual information: bins of the static image on the virtual
+// grid (the values the kernels read) between its minimum and maximum, with the
+// float operations of lc2::mi_bin, and its entropy.
+int set_static_bins(lc2_context* c) {
+  const size_t nv = c->nv;
+  std::vector<float> host(nv);
+  const int ustore = c->cfg.high_res_is_moving ? c->cfg.storage : LC2_STORE_F32;
+  float* tmp = c->d_scratch;  // slot 0
+  LC2_TRY(to_float(c, c->d_static, tmp, nv, ustore));
+  LC2_CUDA(cudaMemcpyAsync(host.data(), tmp, sizeof(float) * nv, cudaMemcpyDeviceToHost, c->stream));
+  LC2_CUDA(cudaStreamSynchronize(c->stream));
+  float lo = host[0], hi = host[0];
+  for (float v : host) {
+    lo = std::min(lo, v);
+    hi = std::max(hi, v);
+  }
+  const float sc = lc2::mi_scale(lo, hi);
+  std::vector<unsigned char> bins(nv);
+  std::vector<long long> counts(lc2::kMiBins, 0);
+  for (size_t i = 0; i < nv; ++i) {
+    const float t = (host[i] - lo) * sc;
+    int b = (int)std::round(t);
+    b = std::min(std::max(b, 0), lc2::kMiBins - 1);
+    bins[i] = (unsigned char)b;
+    ++counts[b];
+  }
+  double s = 0.0;
+  for (long long n : counts)
+    if (n) s += (double)n * std::log((double)n);
+  c->h_static = std::log((double)nv) - s / (double)nv;
+  LC2_CUDA(cudaMemcpyAsync(c->d_sbin, bins.data(), nv, cudaMemcpyHostToDevice, c->stream));
+  LC2_CUDA(cudaStreamSynchronize(c->stream));
+  c->ready = true;
+  return LC2_OK;
+}
+
 // fmax: the fixed image's largest |value| (image_absmax).
 int set_fixed(lc2_context* c, const float* fixed, float fmax, float mmax) {
   const int storage = c->cfg.storage;
@@ -764,6 +877,7 @@ int set_fixed(lc2_context* c, const float* fixed, float fmax, float mmax) {
     LC2_TRY(launch_sobel(c, (const float*)c->d_static, c->d_gstatic, 1, 0));
   }
   LC2_CUDA(cudaStreamSynchronize(c->stream));
+  if (c->mi) return set_static_bins(c);
 
   // fixed-point scales and thresholds
   const float tiny = 1e-30f;
@@ -873,9 +987,13 @@ int stage_host(lc2_context* c, const float* matrices, int count) {
 int enqueue_batch(lc2_context* c, int count) {
   LC2_CUDA(cudaMemcpyAsync(c->d_xf, c->h_xf, sizeof(lc2::Xform) * count, cudaMemcpyHostToDevice,
                            c->stream));
-  LC2_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2 * count, c->stream));
-  LC2_TRY(launch_fused(c, 0, count, nullptr));
-  LC2_TRY(launch_finalize(c, count));
+  if (c->mi) {
+    LC2_TRY(launch_mi(c, count));
+  } else {
+    LC2_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2 * count, c->stream));
+    LC2_TRY(launch_fused(c, 0, count, nullptr));
+    LC2_TRY(launch_finalize(c, count));
+  }
   LC2_CUDA(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(double) * count, cudaMemcpyDeviceToHost,
                            c->stream));
   return LC2_OK;
@@ -913,7 +1031,9 @@ int launch_batch_graph(lc2_context* c, int count) {
     g = &c->graphs.back();
   }
   LC2_CUDA(cudaGraphLaunch(g->exec, c->stream));
-  c->launches += 2;  // fused kernel and ratio
+  c->launches += c->mi ? 2 * ((count + std::max(1, 65535 / c->virt.dim[2]) - 1) /
+                              std::max(1, 65535 / c->virt.dim[2])) + 1
+                       : 2;  // kernels in the graph
   ++c->graph_launches;
   return LC2_OK;
 }
@@ -940,6 +1060,7 @@ int lc2_launch_staged(lc2_context* c, int count) {
     return fail(LC2_ERR_INVALID_ARGUMENT, "launch of %d transforms but %d staged", count, c->staged);
   if (count == 0) return LC2_OK;
   LC2_TRY(select_device(c));
+  if (c->mi) return launch_mi(c, count);
   LC2_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2 * count, c->stream));
   // the fused path keeps nothing per transform on the device, so one launch
   // covers the whole batch; the generic path is bounded by its scratch slots
@@ -968,7 +1089,7 @@ int lc2_evaluate_batch(lc2_context* c, const float* matrices, int count, double*
   g_err.clear();
   LC2_TRY(check_ctx(c));
   if (count > 0 && !out) return fail(LC2_ERR_INVALID_ARGUMENT, "null output");
-  if (c->cfg.high_res_is_moving && c->use_graphs && !c->timing && count > 0) {
+  if ((c->cfg.high_res_is_moving || c->mi) && c->use_graphs && !c->timing && count > 0) {
     LC2_TRY(select_device(c));
     LC2_TRY(stage_host(c, matrices, count));
     c->staged = count;
@@ -991,6 +1112,7 @@ int lc2_evaluate(lc2_context* c, const float* matrix, double* out) {
 
 int lc2_evaluate_fields(lc2_context* c, const float* matrix, double* lc2_out, float* U, float* M,
                         float* G, float* sigma, float* measure) {
+  if (c && c->mi) return fail(LC2_ERR_UNSUPPORTED, "field dumps are LC2 diagnostics (PatchSize >= 1)");
   LC2_TRY(lc2_stage_transforms(c, matrix, 1));
   LC2_TRY(select_device(c));
   const size_t nv = c->nv;
@@ -1510,7 +1632,7 @@ extern "C" int lc2_autotune(lc2_context* c, const float* matrices, int count, in
   if (count < 1) return fail(LC2_ERR_INVALID_ARGUMENT, "autotune needs at least one transform");
   LC2_TRY(select_device(c));
   const int r = c->cfg.patch_size;
-  if (c->lc2_nd == 3 && c->cfg.high_res_is_moving) {
+  if (c->lc2_nd == 3 && c->cfg.high_res_is_moving && !c->mi) {
     LC2_TRY(lc2_stage_transforms(c, matrices, count));
     std::vector<int> rows = (r <= 4) ? std::vector<int>{16, 8} : std::vector<int>{8};
     const int vz = c->virt.dim[2];

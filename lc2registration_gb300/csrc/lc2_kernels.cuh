@@ -92,73 +92,84 @@ __device__ __forceinline__ Axis make_axis(int base, float q, int dim) {
   return a;
 }
 
+// Tile base of a 32 x 8 tile (x0, y0) of slice z: the moving-pixel
+// coordinate in double, split into integer part and fraction, plus the float
+// step matrix. Each voxel adds a float offset of at most (31, 7) voxels to the
+// base fraction, so the interpolation weights keep ~1e-6 voxel accuracy
+// anywhere in the grid.
+struct TileBase {
+  int ib[3];
+  float fb[3];
+  float A[9];
+};
+
+__device__ __forceinline__ void tile_base(const Xform* X, int x0, int y0, int z, TileBase& T) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    double p = X->A[3 * a + 0] * x0 + X->A[3 * a + 1] * y0 + X->A[3 * a + 2] * z + X->b[a];
+    double fl = floor(p);
+    T.ib[a] = (int)fl;
+    T.fb[a] = (float)(p - fl);
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) T.A[i] = (float)X->A[i];
+}
+
+// Trilinear (ND = 3) / bilinear (ND = 2) sample at offset (tx, ty) from the
+// tile base; 0 outside [0, dim-1] (src/Interpolator/interpolator.cu:69-232).
+template <int ND, typename TM>
+__device__ __forceinline__ float tile_sample(const TM* __restrict__ mov, int mx, int my, int mz,
+                                             const TileBase& T, int tx, int ty) {
+  const float dx = (float)tx, dy = (float)ty;
+  if (ND == 3) {
+    float qx = fmaf(T.A[1], dy, fmaf(T.A[0], dx, T.fb[0]));
+    float qy = fmaf(T.A[4], dy, fmaf(T.A[3], dx, T.fb[1]));
+    float qz = fmaf(T.A[7], dy, fmaf(T.A[6], dx, T.fb[2]));
+    Axis ax = make_axis(T.ib[0], qx, mx);
+    Axis ay = make_axis(T.ib[1], qy, my);
+    Axis az = make_axis(T.ib[2], qz, mz);
+    if (!(ax.ok && ay.ok && az.ok)) return 0.0f;
+    const size_t sy = (size_t)mx, sz = (size_t)mx * my;
+    const size_t zf = az.f * sz, zc = az.c * sz, yf = ay.f * sy, yc = ay.c * sy;
+    // z, then y, then x (interpolator.cu:96-128)
+    float lu0 = ldf(mov, ax.f + yf + zf), lu1 = ldf(mov, ax.f + yf + zc);
+    float ru0 = ldf(mov, ax.c + yf + zf), ru1 = ldf(mov, ax.c + yf + zc);
+    float rb0 = ldf(mov, ax.c + yc + zf), rb1 = ldf(mov, ax.c + yc + zc);
+    float lb0 = ldf(mov, ax.f + yc + zf), lb1 = ldf(mov, ax.f + yc + zc);
+    float lu = fmaf(az.r, lu1 - lu0, lu0), ru = fmaf(az.r, ru1 - ru0, ru0);
+    float rb = fmaf(az.r, rb1 - rb0, rb0), lb = fmaf(az.r, lb1 - lb0, lb0);
+    float l = fmaf(ay.r, lb - lu, lu), r = fmaf(ay.r, rb - ru, ru);
+    return fmaf(ax.r, r - l, l);
+  }
+  float qx = fmaf(T.A[1], dy, fmaf(T.A[0], dx, T.fb[0]));
+  float qy = fmaf(T.A[4], dy, fmaf(T.A[3], dx, T.fb[1]));
+  Axis ax = make_axis(T.ib[0], qx, mx);
+  Axis ay = make_axis(T.ib[1], qy, my);
+  if (!(ax.ok && ay.ok)) return 0.0f;
+  const size_t yf = (size_t)ay.f * mx, yc = (size_t)ay.c * mx;
+  // y, then x (interpolator.cu:199-207)
+  float f0 = ldf(mov, ax.f + yf), f1 = ldf(mov, ax.f + yc);
+  float c0 = ldf(mov, ax.c + yf), c1 = ldf(mov, ax.c + yc);
+  float xl = fmaf(ay.r, f1 - f0, f0), xr = fmaf(ay.r, c1 - c0, c0);
+  return fmaf(ax.r, xr - xl, xl);
+}
+
 // One CTA = 32x8 virtual voxels of one z-slice of one transform slot.
-// The tile's base coordinate is computed once in double by thread 0; each
-// voxel adds a float offset of at most ~40 voxels to the base fraction, so
-// the interpolation weights keep ~1e-6 voxel accuracy anywhere in the grid.
 template <int ND, typename TM>
 __global__ void __launch_bounds__(256) k_warp(const TM* __restrict__ mov, int mx, int my, int mz,
                                                int vx, int vy, int vz,
                                                const Xform* __restrict__ xf, int k0,
                                                float* __restrict__ out, size_t slot_stride) {
-  __shared__ int s_base[3];
-  __shared__ float s_frac[3];
-  __shared__ float s_A[9];
+  __shared__ TileBase T;
   const int slot = blockIdx.z / vz;
   const int z = blockIdx.z - slot * vz;
   const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 8;
-  const Xform* X = xf + k0 + slot;
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      double p = X->A[3 * a + 0] * x0 + X->A[3 * a + 1] * y0 + X->A[3 * a + 2] * z + X->b[a];
-      double fl = floor(p);
-      s_base[a] = (int)fl;
-      s_frac[a] = (float)(p - fl);
-    }
-#pragma unroll
-    for (int i = 0; i < 9; ++i) s_A[i] = (float)X->A[i];
-  }
+  if (threadIdx.x == 0 && threadIdx.y == 0) tile_base(xf + k0 + slot, x0, y0, z, T);
   __syncthreads();
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int x = x0 + tx, y = y0 + ty;
   if (x >= vx || y >= vy) return;
-  const float dx = (float)tx, dy = (float)ty;
-  float v = 0.0f;
-  if (ND == 3) {
-    float qx = fmaf(s_A[1], dy, fmaf(s_A[0], dx, s_frac[0]));
-    float qy = fmaf(s_A[4], dy, fmaf(s_A[3], dx, s_frac[1]));
-    float qz = fmaf(s_A[7], dy, fmaf(s_A[6], dx, s_frac[2]));
-    Axis ax = make_axis(s_base[0], qx, mx);
-    Axis ay = make_axis(s_base[1], qy, my);
-    Axis az = make_axis(s_base[2], qz, mz);
-    if (ax.ok && ay.ok && az.ok) {
-      const size_t sx = 1, sy = (size_t)mx, sz = (size_t)mx * my;
-      const size_t zf = az.f * sz, zc = az.c * sz, yf = ay.f * sy, yc = ay.c * sy;
-      // z, then y, then x (interpolator.cu:96-128)
-      float lu0 = ldf(mov, ax.f * sx + yf + zf), lu1 = ldf(mov, ax.f * sx + yf + zc);
-      float ru0 = ldf(mov, ax.c * sx + yf + zf), ru1 = ldf(mov, ax.c * sx + yf + zc);
-      float rb0 = ldf(mov, ax.c * sx + yc + zf), rb1 = ldf(mov, ax.c * sx + yc + zc);
-      float lb0 = ldf(mov, ax.f * sx + yc + zf), lb1 = ldf(mov, ax.f * sx + yc + zc);
-      float lu = fmaf(az.r, lu1 - lu0, lu0), ru = fmaf(az.r, ru1 - ru0, ru0);
-      float rb = fmaf(az.r, rb1 - rb0, rb0), lb = fmaf(az.r, lb1 - lb0, lb0);
-      float l = fmaf(ay.r, lb - lu, lu), r = fmaf(ay.r, rb - ru, ru);
-      v = fmaf(ax.r, r - l, l);
-    }
-  } else {
-    float qx = fmaf(s_A[1], dy, fmaf(s_A[0], dx, s_frac[0]));
-    float qy = fmaf(s_A[4], dy, fmaf(s_A[3], dx, s_frac[1]));
-    Axis ax = make_axis(s_base[0], qx, mx);
-    Axis ay = make_axis(s_base[1], qy, my);
-    if (ax.ok && ay.ok) {
-      const size_t yf = (size_t)ay.f * mx, yc = (size_t)ay.c * mx;
-      // y, then x (interpolator.cu:199-207)
-      float f0 = ldf(mov, ax.f + yf), f1 = ldf(mov, ax.f + yc);
-      float c0 = ldf(mov, ax.c + yf), c1 = ldf(mov, ax.c + yc);
-      float xl = fmaf(ay.r, f1 - f0, f0), xr = fmaf(ay.r, c1 - c0, c0);
-      v = fmaf(ax.r, xr - xl, xl);
-    }
-  }
+  const float v = tile_sample<ND, TM>(mov, mx, my, mz, T, tx, ty);
   out[slot * slot_stride + ((size_t)z * vy + y) * vx + x] = v;
 }
 

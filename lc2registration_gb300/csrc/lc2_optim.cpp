@@ -396,6 +396,7 @@ struct RegObjective {
   std::vector<double> lc2;
   long long evaluations = 0;
   int stage = 0;  // 0 = DIRECT, r + 1 = local round r
+  bool maximize = false;  // NMI (PatchSize 0): maximise the value itself
 };
 
 int params_of(int mode) { return mode == LC2_MODE_2D ? 6 : 12; }
@@ -452,7 +453,11 @@ int reg_objective(void* user, int count, int dim, const double* x, double* f) {
   if (st != LC2_OK) return st;
   for (int k = 0; k < count; ++k) {
     const double v = o->lc2[k];
-    f[k] = (v > 0.0) ? -std::log(v) : std::numeric_limits<double>::max();
+    // -log(LC2) (optimizers.cu:728), or the NMI maximised as it is (:722-724, 855-860)
+    if (o->maximize)
+      f[k] = -v;
+    else
+      f[k] = (v > 0.0) ? -std::log(v) : std::numeric_limits<double>::max();
   }
   if (o->reg->observer) {
     const int np = params_of(mode);
@@ -485,6 +490,11 @@ extern "C" int lc2_register(lc2_context* ctx, const lc2_registration* reg,
   RegObjective o;
   o.ctx = ctx;
   o.reg = reg;
+  o.maximize = reg->maximize != 0;
+  if (ctx) {
+    lc2_config cfg;
+    if (lc2_get_config(ctx, &cfg) == LC2_OK && cfg.patch_size == 0) o.maximize = true;
+  }
   o.base.assign(reg->initial, reg->initial + np);
   int launches = 0;
   auto stage = [&](int algorithm, int mask, double xtol, int maxeval) -> int {

@@ -485,3 +485,50 @@ void or_affine2d(double rot, const double trans[2], const double scale[2], doubl
     }
     out[6] = 0.0f; out[7] = 0.0f; out[8] = 1.0f;
 }
+
+/* ---------------------------------------------------------------- NMI */
+
+static void nmi_bins(const float* v, long long n, int* bins) {
+    float lo = v[0], hi = v[0];
+    for (long long i = 1; i < n; ++i) {
+        if (v[i] < lo) lo = v[i];
+        if (v[i] > hi) hi = v[i];
+    }
+    const float s = hi > lo ? 255.0f / (hi - lo) : 0.0f;
+    for (long long i = 0; i < n; ++i) {
+        const float t = (v[i] - lo) * s;
+        int b = (int)roundf(t);
+        bins[i] = b < 0 ? 0 : (b > 255 ? 255 : b);
+    }
+}
+
+static double entropy_of_counts(const long long* c, int nb, double n) {
+    double s = 0.0;
+    for (int i = 0; i < nb; ++i)
+        if (c[i]) s += (double)c[i] * log((double)c[i]);
+    return log(n) - s / n;
+}
+
+double or_nmi(const float* U, const float* H, long long n) {
+    int* bu = (int*)malloc(sizeof(int) * (size_t)n);
+    int* bh = (int*)malloc(sizeof(int) * (size_t)n);
+    long long* joint = (long long*)calloc(256 * 256, sizeof(long long));
+    long long cu[256] = {0}, ch[256] = {0};
+    if (!bu || !bh || !joint) {
+        free(bu); free(bh); free(joint);
+        return 0.0;
+    }
+    nmi_bins(U, n, bu);
+    nmi_bins(H, n, bh);
+    for (long long i = 0; i < n; ++i) {
+        ++joint[bu[i] + 256 * bh[i]];
+        ++cu[bu[i]];
+        ++ch[bh[i]];
+    }
+    const double hu = entropy_of_counts(cu, 256, (double)n);
+    const double hh = entropy_of_counts(ch, 256, (double)n);
+    const double hj = entropy_of_counts(joint, 256 * 256, (double)n);
+    free(bu); free(bh); free(joint);
+    const double v = (hu + hh) / hj;
+    return isfinite(v) ? v : 0.0;
+}

@@ -18,6 +18,7 @@
  *                    minimum-norm solution, i.e. the projection onto the span
  *                    of the non-degenerate centred columns)
  *   or_lc2_*         src/cu_LC2/cu_lc2_2d.cu:599-653, cu_lc2_3d.cu:1119-1194
+ *   or_nmi           src/cu_LC2/cu_lc2_3d.cu:868-923, 1196-1301 (PatchSize 0)
  *
  * All arithmetic is IEEE double. Inputs are float32 volumes, x fastest
  * (index x + y*X + z*X*Y), exactly as the reference stores them.
@@ -92,6 +93,14 @@ double or_lc2_eval(int resample_ndim, int lc2_ndim, const or_geom* fixed_g, cons
                    int r, int hr_moving, const float* mat, int use_boxsum, int nthreads,
                    double* U_out, double* M_out, double* G_out, double* sigma_out,
                    double* measure_out, double* sums_out);
+
+/* Normalised mutual information of two float images of n voxels
+ * (src/cu_LC2/cu_lc2_3d.cu:868-923, 1196-1301): 256 bins per image between
+ * its own min and max, bin = roundf((v - min) * s) with s = 255 / (max - min)
+ * in float arithmetic (s = 0 when max == min), joint histogram
+ * U-bin + 256 * H-bin, H(X) = -sum p ln p with p = count / n in double.
+ * Returns (H(U) + H(H)) / H(U, H), 0 when not finite. */
+double or_nmi(const float* U, const float* H, long long n);
 
 /* Virtual grid per src/Interpolator/interpolator.cu:337-339: origin = fixed
  * origin, dims = ceil(dimF*spF/spV) (float arithmetic as in the reference). */

@@ -92,6 +92,8 @@ def _load():
                                 _dp, _dp, _dp]
     lib.or_virtual_geom.argtypes = [ctypes.c_int, gp, _fp, gp]
     lib.or_affine3d.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _fp]
+    lib.or_nmi.restype = ctypes.c_double
+    lib.or_nmi.argtypes = [_fp, _fp, ctypes.c_longlong]
     lib.or_affine2d.argtypes = [ctypes.c_double, _dp, _dp, ctypes.c_double, _dp, _dp, _fp]
     _lib = lib
     return lib
@@ -209,6 +211,26 @@ def lc2_eval(mode: str, fixed_geom: Geom, fixed: np.ndarray, moving_geom: Geom,
         return float(val)
     U, M, G, sg, ms = outs
     return float(val), dict(U=U, M=M, G=G, sigma=sg, measure=ms, sums=sums, virt=vg)
+
+
+def nmi(U: np.ndarray, H: np.ndarray) -> float:
+    """Normalised mutual information of two float images (or_nmi)."""
+    lib = _load()
+    u, h = _f32(U).ravel(), _f32(H).ravel()
+    return float(lib.or_nmi(_ptr(u, _fp), _ptr(h, _fp), ctypes.c_longlong(u.size)))
+
+
+def nmi_eval(fixed_geom: Geom, fixed: np.ndarray, moving_geom: Geom, moving: np.ndarray,
+             virt_spacing: Sequence[float], mat, hr_moving: bool = True) -> float:
+    """NMI of a 3D evaluation (PatchSize 0): fixed resampled through the
+    identity and moving through ``mat`` onto the virtual grid, rounded to
+    float32 as the device holds them; the ultrasound is the fixed image when
+    hr_moving."""
+    vg = virtual_geom(3, fixed_geom, virt_spacing)
+    eye = np.eye(4, dtype=np.float32)
+    F = resample(3, vg, fixed_geom, fixed, eye).astype(np.float32)
+    M = resample(3, vg, moving_geom, moving, mat).astype(np.float32)
+    return nmi(F, M) if hr_moving else nmi(M, F)
 
 
 def affine3d(rot, trans, scale, shear, center, shift) -> np.ndarray:

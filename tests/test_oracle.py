@@ -137,3 +137,14 @@ def test_virtual_geometry_matches_reference_formula():
     assert v.dim[:2] == [164, 151]  # config/Data/fixed.bin is 164 x 151
     v = O.virtual_geom(2, g, (0.9, 0.9))
     assert v.dim[:2] == [182, 168]  # *_virtual.bin is 182 x 168
+
+
+def test_nmi_known_values():
+    rng = np.random.default_rng(0)
+    U = rng.random(4000).astype(np.float32)
+    assert abs(O.nmi(U, U) - 2.0) < 1e-12           # identical images
+    assert abs(O.nmi(U, 3 * U + 1) - 2.0) < 1e-12   # affine intensity map, same bins
+    c = np.full(4000, 0.5, dtype=np.float32)
+    assert O.nmi(U, c) == 1.0                        # constant image: H = 0, H(U,M) = H(U)
+    V = rng.random(4000).astype(np.float32)
+    assert 1.0 < O.nmi(U, V) < O.nmi(U, 0.5 * U + 0.1 * V)
