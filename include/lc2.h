@@ -119,6 +119,22 @@ int lc2_set_stream(lc2_context* ctx, void* stream);
 int lc2_evaluate_fields(lc2_context* ctx, const float* matrix, double* lc2_out, float* U,
                         float* M, float* G, float* sigma, float* measure);
 
+/* Weighting map of one evaluation: measure / sigma per virtual voxel, 0
+ * where sigma is not above 1e-6 (LC2_3D_class::GenerateWeightingMap /
+ * CalculateWeightingMap, src/cu_LC2/cu_lc2_3d.cu:843-866, 1303-1329; here
+ * for 2D grids too). map: virtual-grid floats; *lc2_out (may be NULL) the
+ * evaluation's LC2. */
+int lc2_weighting_map(lc2_context* ctx, const float* matrix, double* lc2_out, float* map);
+
+/* The registered 2D image: src (sw x sh) warped into dst (dw x dh) by the
+ * forward pixel map (x', y') = C (x, y, 1), coeffs = C's two rows, bilinear,
+ * destination pixels whose source falls outside src left at 0. Replaces the
+ * nppiWarpAffine_32f_C1R call of Interpolator2D::WriteOut
+ * (src/Interpolator/interpolator.cu:1438-1535). Host buffers; runs on
+ * `device`. */
+int lc2_warp_affine_2d(const float* src, int sw, int sh, float* dst, int dw, int dh,
+                       const double coeffs[6], int device);
+
 /* Kernel launches issued by this context since creation (device work
  * accounting for benchmarks). */
 long long lc2_launch_count(const lc2_context* ctx);

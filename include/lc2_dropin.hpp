@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "lc2.h"
+#include "lc2_io.hpp"
 #include "lc2_yaml.hpp"
 
 #include <algorithm>
@@ -270,6 +271,7 @@ class InterpolatorBase {
   Context ctx_;
   Volume fixed_vol_, moving_vol_;  // owned images (parameter-file constructors)
   std::string output_path_;
+  std::string fixed_path_, moving_path_;  // FilePath of the parameter file, if any
 
  public:
   // Mapper centre and shift of InitiateMappers (for the registration driver).
@@ -364,6 +366,8 @@ class Interpolator3D : public InterpolatorBase {
     const lc2yaml::Node& rp = in["RegistrationParameters"];
     fixed_vol_ = load_volume(in["FixedVolume"], 3);
     moving_vol_ = load_volume(in["MovingVolume"], 3);
+    fixed_path_ = in["FixedVolume"]["FilePath"].str();
+    moving_path_ = in["MovingVolume"]["FilePath"].str();
     cfg_.mode = mode;
     for (int a = 0; a < 3; ++a) {
       cfg_.fixed.dim[a] = fixed_vol_.dim[a];
@@ -422,6 +426,62 @@ class Interpolator3D : public InterpolatorBase {
     GenerateMappers(RotationAngle, Translation, scale, shear);
     GetCurrentTransform(out);
   }
+
+  // Virtual-grid volumes of the current transform (interpolator.cu:681-729):
+  // <fixed name>.nrrd holds the high-resolution image, <moving name>_Registered.nrrd
+  // the ultrasound, both at the virtual spacing with origin (0,0,0).
+  void WriteOut() {
+    if (!handle_ready_) throw Error(LC2_ERR_NOT_READY, "InitiateRegistrationHandle not called");
+    int d[3];
+    check(lc2_virtual_dims(ctx_.get(), d), "lc2_virtual_dims");
+    const size_t n = (size_t)d[0] * d[1] * d[2];
+    std::vector<float> U(n), M(n);
+    double v = 0.0;
+    check(lc2_evaluate_fields(ctx_.get(), matrix_.data(), &v, U.data(), M.data(), nullptr,
+                              nullptr, nullptr),
+          "lc2_evaluate_fields");
+    lc2io::NrrdHeader h{};
+    for (int a = 0; a < 3; ++a) {
+      h.sizes[a] = d[a];
+      h.directions[a][a] = cfg_.virtual_spacing[a];
+    }
+    lc2io::write_nrrd(output_path_ + lc2io::stem_with_slash(fixed_path_, "fixed") + ".nrrd", h,
+                      M.data());
+    lc2io::write_nrrd(
+        output_path_ + lc2io::stem_with_slash(moving_path_, "moving") + "_Registered.nrrd", h,
+        U.data());
+  }
+
+  // The moving volume with the optimal moving->fixed matrix applied to its
+  // axes and origin, <moving name>_Registered.nrrd, and the matrix itself as
+  // MovingToFixed.mat (interpolator.cu:738-849). Float accumulation in the
+  // reference's order.
+  void WriteOut(float* OptimizedMatrix) {
+    const float* m = OptimizedMatrix;
+    lc2io::NrrdHeader h{};
+    for (int a = 0; a < 3; ++a) h.sizes[a] = cfg_.moving.dim[a];
+    for (int a = 0; a < 3; ++a) {  // axis a: M * (spacing_a e_a)
+      float axis[3] = {0.0f, 0.0f, 0.0f};
+      axis[a] = cfg_.moving.spacing[a];
+      for (int row = 0; row < 3; ++row) {
+        float acc = 0.0f;
+        for (int e = 0; e < 3; ++e) acc += m[e + row * 4] * axis[e];
+        h.directions[a][row] = acc;
+      }
+    }
+    const float o4[4] = {cfg_.moving.origin[0], cfg_.moving.origin[1], cfg_.moving.origin[2],
+                         1.0f};
+    for (int row = 0; row < 3; ++row) {
+      float acc = 0.0f;
+      for (int e = 0; e < 4; ++e) acc += m[e + row * 4] * o4[e];
+      h.origin[row] = acc;
+    }
+    if (!moving_) throw Error(LC2_ERR_NOT_READY, "no moving volume");
+    lc2io::write_nrrd(
+        output_path_ + lc2io::stem_with_slash(moving_path_, "moving") + "_Registered.nrrd", h,
+        moving_);
+    lc2io::write_matrix(output_path_ + "/MovingToFixed.mat", m, 4, 4);
+  }
 };
 
 // 2D frame (US, z = 1) against a 3D volume; the LC2 runs on the frame.
@@ -431,6 +491,8 @@ class Interpolator2DTo3D : public Interpolator3D {
       : Interpolator3D(c, LC2_MODE_2DTO3D) {}
   explicit Interpolator2DTo3D(const std::string& yaml_path)
       : Interpolator3D(yaml_path, false, LC2_MODE_2DTO3D) {}
+  // the reference writes nothing here (interpolator.cu:1777-1785)
+  void WriteOut() {}
 };
 
 // 2D registration.
@@ -468,6 +530,8 @@ class Interpolator2D : public InterpolatorBase {
     const lc2yaml::Node& rp = in["RegistrationParameters"];
     fixed_vol_ = load_volume(in["FixedImage"], 2);
     moving_vol_ = load_volume(in["MovingImage"], 2);
+    fixed_path_ = in["FixedImage"]["FilePath"].str();
+    moving_path_ = in["MovingImage"]["FilePath"].str();
     cfg_.mode = LC2_MODE_2D;
     for (int a = 0; a < 2; ++a) {
       cfg_.fixed.dim[a] = fixed_vol_.dim[a];
@@ -528,6 +592,55 @@ class Interpolator2D : public InterpolatorBase {
     out[6] = 0.0f;
     out[7] = 0.0f;
     out[8] = 1.0f;
+  }
+
+  // the reference writes nothing here (interpolator.cu:1427-1436)
+  void WriteOut() {}
+
+  // The moving image registered into the fixed image's pixel grid with the
+  // optimal moving->fixed matrix, converted to pixel units exactly as the
+  // reference does (interpolator.cu:1438-1535), written as
+  // <moving name>_Registered.png (values rounded, outside [0, 255] -> 0) or,
+  // when a value exceeds 255, as raw float32 <moving name>_Registered.raw.
+  // Returns the path written.
+  std::string WriteOut(float* OptimizedMatrix) {
+    if (!moving_) throw Error(LC2_ERR_NOT_READY, "no moving image");
+    double A[2][3];
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 3; ++j) A[i][j] = OptimizedMatrix[j + i * 3];
+    const lc2_geometry& F = cfg_.fixed;
+    const lc2_geometry& Mv = cfg_.moving;
+    A[0][2] /= F.spacing[0];
+    A[1][2] /= F.spacing[1];
+    A[0][0] *= (Mv.spacing[0] / F.spacing[0]);
+    A[1][0] *= (Mv.spacing[0] / F.spacing[0]);
+    A[0][1] *= (Mv.spacing[1] / F.spacing[1]);
+    A[1][1] *= (Mv.spacing[1] / F.spacing[1]);
+    const double coeffs[6] = {A[0][0], A[0][1], A[0][2], A[1][0], A[1][1], A[1][2]};
+    const int fw = F.dim[0], fh = F.dim[1];
+    std::vector<float> reg((size_t)fw * fh);
+    check(lc2_warp_affine_2d(moving_, Mv.dim[0], Mv.dim[1], reg.data(), fw, fh, coeffs,
+                             cfg_.device),
+          "lc2_warp_affine_2d");
+    float mx = reg.empty() ? 0.0f : reg[0];
+    for (float v : reg) mx = std::max(mx, v);
+    const std::string base = output_path_ + lc2io::stem_with_slash(moving_path_, "moving");
+    if (mx > 255.0f) {
+      const std::string path = base + "_Registered.raw";
+      std::ofstream f(path, std::ios::out | std::ios::binary);
+      if (!f) throw Error(LC2_ERR_INVALID_ARGUMENT, "cannot write " + path);
+      f.write(reinterpret_cast<const char*>(reg.data()),
+              (std::streamsize)(reg.size() * sizeof(float)));
+      return path;
+    }
+    std::vector<uint8_t> px(reg.size());
+    for (size_t i = 0; i < reg.size(); ++i) {
+      const float v = reg[i];
+      px[i] = (v > 255.0f || v < 0.0f) ? 0 : (uint8_t)std::roundf(v);
+    }
+    const std::string path = base + "_Registered.png";
+    lc2io::write_png_gray8(path, fw, fh, px.data());
+    return path;
   }
 };
 

@@ -43,7 +43,8 @@ EXPORTED = [
     "lc2_stack_launch_count", "lc2_stack_graph_launches", "lc2_context_bytes",
     "lc2_server_create", "lc2_server_submit", "lc2_server_poll", "lc2_server_drain",
     "lc2_server_get_stats", "lc2_server_reset_stats", "lc2_server_destroy",
-    "lc2_graph_launches", "lc2_autotune", "lc2_get_config",
+    "lc2_graph_launches", "lc2_autotune", "lc2_get_config", "lc2_weighting_map",
+    "lc2_warp_affine_2d",
 ]
 
 ALGORITHMS = {"direct_l": 1, "bobyqa": 2, "nelder_mead": 3}
@@ -203,6 +204,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "lc2_server_destroy": ([vp], ctypes.c_int),
         "lc2_graph_launches": ([vp], ctypes.c_longlong),
         "lc2_get_config": ([vp, ctypes.POINTER(lc2_config)], ctypes.c_int),
+        "lc2_weighting_map": ([vp, _fp, _dp, _fp], ctypes.c_int),
+        "lc2_warp_affine_2d": ([_fp, ctypes.c_int, ctypes.c_int, _fp, ctypes.c_int, ctypes.c_int,
+                                _dp, ctypes.c_int], ctypes.c_int),
         "lc2_autotune": ([vp, _fp, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                           ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
     }
@@ -344,6 +348,16 @@ class Context:
     def set_option(self, option: int, value: int):
         _check(self._lib.lc2_set_option(self._h, int(option), int(value)))
 
+    def weighting_map(self, mat):
+        """(lc2, per-voxel measure / sigma float32 array)."""
+        m = self._mats(mat)
+        d = self.virtual_dims()
+        out = np.empty(d[0] * d[1] * d[2], dtype=np.float32)
+        v = ctypes.c_double()
+        _check(self._lib.lc2_weighting_map(self._h, m.ctypes.data_as(_fp), ctypes.byref(v),
+                                           out.ctypes.data_as(_fp)))
+        return v.value, out
+
     def graph_launches(self) -> int:
         return int(self._lib.lc2_graph_launches(self._h))
 
@@ -454,6 +468,16 @@ class Stack:
     def launch_count(self) -> int:
         return int(self._lib.lc2_stack_launch_count(self._h))
 
+    def weighting_map(self, mat):
+        """(lc2, per-voxel measure / sigma float32 array)."""
+        m = self._mats(mat)
+        d = self.virtual_dims()
+        out = np.empty(d[0] * d[1] * d[2], dtype=np.float32)
+        v = ctypes.c_double()
+        _check(self._lib.lc2_weighting_map(self._h, m.ctypes.data_as(_fp), ctypes.byref(v),
+                                           out.ctypes.data_as(_fp)))
+        return v.value, out
+
     def graph_launches(self) -> int:
         return int(self._lib.lc2_stack_graph_launches(self._h))
 
@@ -473,6 +497,20 @@ def affine_2d(rot, trans, scale=(1, 1), shear=0.0, center=(0, 0), shift=(0, 0)):
     _check(lib.lc2_affine_2d(float(rot), t.ctypes.data_as(_fp), s.ctypes.data_as(_fp), float(shear),
                              c.ctypes.data_as(_fp), sh.ctypes.data_as(_fp), out.ctypes.data_as(_fp)))
     return out.reshape(3, 3)
+
+
+def warp_affine_2d(src: np.ndarray, dst_shape, coeffs, device: int = 0) -> np.ndarray:
+    """lc2_warp_affine_2d: src (h, w) float image warped by the forward pixel
+    map coeffs (2x3) into an array of dst_shape (h', w')."""
+    lib = load()
+    s = _f32(src)
+    sh, sw = s.shape
+    dh, dw = dst_shape
+    out = np.empty((dh, dw), dtype=np.float32)
+    c = np.ascontiguousarray(coeffs, dtype=np.float64).ravel()
+    _check(lib.lc2_warp_affine_2d(s.ctypes.data_as(_fp), sw, sh, out.ctypes.data_as(_fp), dw, dh,
+                                  c.ctypes.data_as(_dp), int(device)))
+    return out
 
 
 def invert_affine_3d(mat) -> np.ndarray:

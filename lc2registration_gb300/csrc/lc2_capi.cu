@@ -1164,6 +1164,53 @@ int lc2_evaluate_fields(lc2_context* c, const float* matrix, double* lc2_out, fl
   return LC2_OK;
 }
 
+namespace lc2 {
+// measure / sigma where sigma > 1e-6, else 0 (cu_lc2_3d.cu:843-866)
+__global__ void k_weight_map(const float* __restrict__ measure, const float* __restrict__ sigma,
+                             size_t n, float* __restrict__ out) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const float s = sigma[i];
+    out[i] = s > 1e-6f ? measure[i] / s : 0.0f;
+  }
+}
+}  // namespace lc2
+
+int lc2_weighting_map(lc2_context* c, const float* matrix, double* lc2_out, float* map) {
+  if (!map) return fail(LC2_ERR_INVALID_ARGUMENT, "null map");
+  if (c && c->mi) return fail(LC2_ERR_UNSUPPORTED, "the weighting map is an LC2 quantity (PatchSize >= 1)");
+  LC2_TRY(lc2_stage_transforms(c, matrix, 1));
+  LC2_TRY(select_device(c));
+  const size_t nv = c->nv;
+  float* buf = nullptr;
+  LC2_CUDA(cudaMalloc(&buf, sizeof(float) * nv * 3));
+  struct Free {
+    float* p;
+    ~Free() { cudaFree(p); }
+  } guard{buf};
+  float* osig = buf;
+  float* omeas = buf + nv;
+  float* dmap = buf + 2 * nv;
+  LC2_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2, c->stream));
+  const float* sig = osig;
+  if (c->cfg.high_res_is_moving) {
+    LC2_TRY(launch_fused(c, 0, 1, omeas));
+    sig = c->d_sigma;
+  } else {
+    LC2_TRY(launch_group_generic(c, 0, 1, osig, omeas));
+  }
+  LC2_TRY(launch_finalize(c, 1));
+  const int blocks = (int)std::min<size_t>((nv + 255) / 256, 152 * 16);
+  lc2::k_weight_map<<<blocks, 256, 0, c->stream>>>(omeas, sig, nv, dmap);
+  ++c->launches;
+  LC2_CUDA(cudaGetLastError());
+  LC2_CUDA(cudaMemcpyAsync(map, dmap, sizeof(float) * nv, cudaMemcpyDeviceToHost, c->stream));
+  LC2_CUDA(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  LC2_CUDA(cudaStreamSynchronize(c->stream));
+  if (lc2_out) *lc2_out = c->h_out[0];
+  return LC2_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Transform builders (host)
 // ---------------------------------------------------------------------------

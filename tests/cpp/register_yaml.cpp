@@ -3,7 +3,9 @@
 //   Interpolator(yaml) -> InitiateMappers -> InitiateRegistrationHandle ->
 //   Optimizers(yaml) -> LinkToInterpolator -> Optimize -> ExportResults.
 //   register_yaml <2D|3D|2DTo3D> <params.yaml>
-// Prints the optimum, LC2 and evaluation count; writes <name>_result.yaml.
+// Prints the optimum, LC2 and evaluation count; writes <name>_result.yaml and,
+// as main.cu does after ExportResults, the registered moving image
+// (WriteOut(OptimalMatrix)).
 // With one argument <params.yaml> it only parses and re-emits the file.
 #include <cstdio>
 #include <iostream>
@@ -31,6 +33,9 @@ int main(int argc, char** argv) {
       o.LinkToInterpolator(&interp);
       o.Optimize();
       o.ExportResults();
+      float OptimalMatrix[9] = {0.0f};
+      o.GetInternalMatrix(OptimalMatrix);
+      interp.WriteOut(OptimalMatrix);
       opt = o.OptimalSolution;
       sim = o.SimilarityMeasure;
       evals = o.EvalCounter;
@@ -43,6 +48,9 @@ int main(int argc, char** argv) {
       o.LinkToInterpolator(&interp);
       o.Optimize();
       o.ExportResults();
+      float OptimalMatrix[16] = {0.0f};
+      o.GetInternalMatrix(OptimalMatrix);
+      interp.WriteOut(OptimalMatrix);
       opt = o.OptimalSolution;
       sim = o.SimilarityMeasure;
       evals = o.EvalCounter;

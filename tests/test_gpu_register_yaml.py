@@ -57,6 +57,25 @@ def _check_files(tmp_path, result, params, sim, evals, keys, mode, case):
     assert log[0].startswith("Step,Transform[16]")
     assert len(log) == 1 + 1 + evals        # header, initial row, one row per evaluation
     assert "Enabled: false" in text          # DIRECT and round 0 disabled for a re-run
+    if mode == "3D":
+        # WriteOut(OptimalMatrix): moving volume with transformed axes/origin, and the matrix
+        from tests.test_io import read_nrrd
+        fields, body = read_nrrd(tmp_path / "moving_Registered.nrrd")
+        np.testing.assert_array_equal(body, case.moving.astype(np.float32).ravel())
+        sp, org = np.array(case.moving_geom.spacing), np.array(case.moving_geom.origin)
+        dirs = [np.array(v.split(","), float) for v in
+                fields["space directions"].strip("()").split(") (")]
+        for a in range(3):
+            np.testing.assert_allclose(dirs[a], tm[:3, a] * sp[a], rtol=2e-5, atol=2e-5)
+        o = np.array(fields["space origin"].strip("()").split(","), float)
+        np.testing.assert_allclose(o, tm[:3, :3] @ org + tm[:3, 3], rtol=2e-5, atol=2e-4)
+        mat = np.array([[float(v) for v in ln.rstrip(",").split(",")]
+                        for ln in open(tmp_path / "MovingToFixed.mat").read().splitlines()])
+        np.testing.assert_allclose(mat, tm, rtol=2e-5, atol=2e-5)
+    else:
+        from tests.test_io import read_png_gray8
+        px = read_png_gray8(tmp_path / "moving_Registered.png")
+        assert px.shape == (case.fixed_geom.dim[1], case.fixed_geom.dim[0])
 
 
 def test_register_yaml_2d(tmp_path):
