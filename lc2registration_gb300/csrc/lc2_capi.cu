@@ -87,6 +87,7 @@ struct lc2_context {
   // static ultrasound (HighResolutionModality: Moving): weighting factor per
   // voxel and its exact fixed-point sum
   float* d_sigma = nullptr;
+  int* d_su = nullptr;  // window sum of the quantised static ultrasound per voxel
   long long sigma_sum = -1;
   // normalised mutual information (patch_size 0): static image bins and
   // entropy, per-transform range and joint histogram
@@ -124,6 +125,33 @@ struct lc2_context {
 };
 
 namespace lc2 {
+// Exact window sum of width 2r+1 along one axis (0 = x, 1 = y, 2 = z) with
+// zero padding; one thread per line of the (nx, ny, nz) grid.
+__global__ void k_box_line(const int* __restrict__ in, int* __restrict__ out, int nx, int ny,
+                           int nz, int axis, int r) {
+  const long long line = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t base, stride;
+  int len;
+  if (axis == 0) {
+    if (line >= (long long)ny * nz) return;
+    base = (size_t)line * nx; stride = 1; len = nx;
+  } else if (axis == 1) {
+    if (line >= (long long)nx * nz) return;
+    base = (size_t)(line / nx) * nx * ny + (size_t)(line % nx); stride = nx; len = ny;
+  } else {
+    if (line >= (long long)nx * ny) return;
+    base = (size_t)line; stride = (size_t)nx * ny; len = nz;
+  }
+  int a = 0;
+  for (int i = 0; i <= r && i < len; ++i) a += in[base + i * stride];
+  out[base] = a;
+  for (int i = 1; i < len; ++i) {
+    if (i + r < len) a += in[base + (size_t)(i + r) * stride];
+    if (i - r - 1 >= 0) a -= in[base + (size_t)(i - r - 1) * stride];
+    out[base + (size_t)i * stride] = a;
+  }
+}
+
 // LC2 = sum(measure) / sum(sigma); 0 when NaN/Inf (cu_lc2_3d.cu:1189-1191).
 // sigma_sum >= 0: the weighting-factor sum is static (precomputed), else it
 // is taken from the accumulator.
@@ -423,6 +451,7 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
   L.mov = c->d_moving;
   L.ust = c->d_static;
   L.sig = c->d_sigma;
+  L.su = c->d_su;
   L.P = c->fp;
   L.xf = c->d_xf;
   L.k0 = k0;
@@ -605,7 +634,7 @@ void context_bytes(const lc2_context* c, size_t* held, size_t* peak_extra) {
   h += c->nm * es;                             // moving
   h += c->nv * (hrm ? es : sizeof(float));     // static image on the virtual grid
   if (!hrm) h += c->nv * sizeof(float);        // its Sobel
-  if (hrm && !c->mi) h += c->nv * sizeof(float);  // weighting factors
+  if (hrm && !c->mi) h += c->nv * (sizeof(float) + sizeof(int));  // weighting factors, S_U
   if (c->mi) h += c->nv + 64 * (sizeof(unsigned) * (lc2::kMiHist + 2));
   h += 64 * (sizeof(lc2::Xform) + 2 * sizeof(unsigned long long) + sizeof(double));
   *held = h;
@@ -639,6 +668,8 @@ int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
     e = cudaMalloc(&c->d_gstatic, c->nv * sizeof(float));
   if (e == cudaSuccess && cfg->high_res_is_moving && !c->mi)
     e = cudaMalloc(&c->d_sigma, c->nv * sizeof(float));
+  if (e == cudaSuccess && cfg->high_res_is_moving && !c->mi)
+    e = cudaMalloc(&c->d_su, c->nv * sizeof(int));
   if (e == cudaSuccess && c->mi) e = cudaMalloc(&c->d_sbin, c->nv);
   if (e != cudaSuccess) {
     lc2_destroy(c);
@@ -683,6 +714,7 @@ int lc2_destroy(lc2_context* c) {
   cudaFree(c->d_static);
   cudaFree(c->d_gstatic);
   cudaFree(c->d_sigma);
+  cudaFree(c->d_su);
   cudaFree(c->d_scratch);
   drop_graphs(c);
   cudaFree(c->d_sbin);
@@ -810,6 +842,39 @@ int upload_image(lc2_context* c, const float* host, size_t n, void* dst, int sto
 // largest |value| (its scale enters the fixed-point parameters): the fixed
 // image on the virtual grid, the fixed-point parameters and, for a static
 // ultrasound, the weighting factors and their sum.
+// Window sums of the quantised static ultrasound per voxel (the S_U of the
+// fused kernels), by exact separable passes through scratch slot 0.
+int static_window_sum(lc2_context* c) {
+  const lc2_geometry& v = c->virt;
+  const size_t nv = c->nv;
+  int* ta = reinterpret_cast<int*>(c->d_scratch);
+  int* tb = ta + nv;  // the slot holds two planes of nv floats
+  const int blocks = (int)std::min<size_t>((nv + 255) / 256, 152 * 16);
+  const int st = c->cfg.storage;
+  if (st == LC2_STORE_F16)
+    lc2::k_quant_static<__half><<<blocks, 256, 0, c->stream>>>((const __half*)c->d_static, nv, c->fp.qu, ta);
+  else if (st == LC2_STORE_BF16)
+    lc2::k_quant_static<__nv_bfloat16><<<blocks, 256, 0, c->stream>>>((const __nv_bfloat16*)c->d_static, nv, c->fp.qu, ta);
+  else
+    lc2::k_quant_static<float><<<blocks, 256, 0, c->stream>>>((const float*)c->d_static, nv, c->fp.qu, ta);
+  const int nx = v.dim[0], ny = v.dim[1], nz = v.dim[2], r = c->cfg.patch_size;
+  auto pass = [&](const int* in, int* out, int axis, long long lines) {
+    lc2::k_box_line<<<(unsigned)((lines + 127) / 128), 128, 0, c->stream>>>(in, out, nx, ny, nz,
+                                                                            axis, r);
+  };
+  pass(ta, tb, 0, (long long)ny * nz);
+  if (c->lc2_nd == 3) {
+    pass(tb, ta, 1, (long long)nx * nz);
+    pass(ta, c->d_su, 2, (long long)nx * ny);
+  } else {
+    pass(tb, c->d_su, 1, (long long)nx * nz);
+  }
+  c->launches += (c->lc2_nd == 3) ? 4 : 3;
+  LC2_CUDA(cudaGetLastError());
+  LC2_CUDA(cudaStreamSynchronize(c->stream));
+  return LC2_OK;
+}
+
 // Normalised mutual information: bins of the static image on the virtual
 // grid (the values the kernels read) between its minimum and maximum, with the
 // float operations of lc2::mi_bin, and its entropy.
@@ -941,6 +1006,7 @@ int set_fixed(lc2_context* c, const float* fixed, float fmax, float mmax) {
     LC2_CUDA(cudaMemcpyAsync(sums, c->d_acc, sizeof(sums), cudaMemcpyDeviceToHost, c->stream));
     LC2_CUDA(cudaStreamSynchronize(c->stream));
     c->sigma_sum = (long long)sums[1];
+    LC2_TRY(static_window_sum(c));
   }
   c->ready = true;
   return LC2_OK;
@@ -1606,6 +1672,7 @@ int lc2_stack_evaluate(lc2_stack* s, int count, const int* frame_ids, const floa
       S.mov = s->d_moving;
       S.ust = c->d_static;
       S.sig = c->d_sigma;
+      S.su = c->d_su;
       S.P = c->fp;
       S.P.ntx = (c->virt.dim[0] + 31) / 32;
       S.P.zchunk = 1;

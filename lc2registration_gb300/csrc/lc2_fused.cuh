@@ -16,9 +16,11 @@
 //   4. solves each output voxel's least-squares fit against the precomputed
 //      weighting factor sigma (cu_lc2_3d.cu:526-618) and adds its clipped
 //      measure to the transform's exact fixed-point sum.
-// Fields are 13 int32 limbs: qU, qM, qG, and the 64-bit products UM, UG, MM,
-// GG, MG split as hi * 2^K + lo (0 <= lo < 2^K); every limb's window sum fits
+// Fields are 12 int32 limbs: qM, qG, and the 64-bit products UM, UG, MM, GG,
+// MG split as hi * 2^K + lo (0 <= lo < 2^K); every limb's window sum fits
 // int32, so each running update is one 32-bit add and all sums stay exact.
+// The ultrasound is static, so its window sum S_U is precomputed once per
+// context (su) like the weighting factor.
 // Nothing per voxel is written to global memory, so the moving volume stays
 // resident in L2 while many transforms are evaluated.
 // ND = 2 covers the 2D and 2D-to-3D modes (one slice, no z window); WND is the
@@ -42,7 +44,7 @@ struct FusedParams {
   float sum_scale;         // fixed-point scale of the measure sum
 };
 
-constexpr int kLimbs = 13;
+constexpr int kLimbs = 12;
 
 // Compile-time geometry of one fused CTA: a 32 x TY output tile, patch radius R.
 template <int ND, int TY, int R>
@@ -104,21 +106,21 @@ __device__ __forceinline__ float fused_sample(const TM* __restrict__ mov, const 
   return fmaf(ax.r, xr - xl, xl);
 }
 
-// 13 limbs of one point's moment fields: qU, qM, qG, then (lo, hi) of the
+// 12 limbs of one point's moment fields: qM, qG, then (lo, hi) of the
 // products UM, UG, MM, GG, MG split as hi * 2^K + lo.
 __device__ __forceinline__ void fused_limbs(int qu, int qm, int qg, int K, int* L) {
   const unsigned long long mask = (1ull << K) - 1ull;
   const long long p[5] = {(long long)qu * qm, (long long)qu * qg, (long long)qm * qm,
                           (long long)qg * qg, (long long)qm * qg};
-  L[0] = qu;
-  L[1] = qm;
-  L[2] = qg;
+  L[0] = qm;
+  L[1] = qg;
 #pragma unroll
   for (int i = 0; i < 5; ++i) {
-    L[3 + 2 * i] = (int)((unsigned long long)p[i] & mask);
-    L[4 + 2 * i] = (int)(p[i] >> K);
+    L[2 + 2 * i] = (int)((unsigned long long)p[i] & mask);
+    L[3 + 2 * i] = (int)(p[i] >> K);
   }
 }
+
 
 // x and y window passes in place on the limb planes A: after them, A rows
 // < TY, columns < 32 hold the patch sums. One thread per (limb, row), then
@@ -208,6 +210,16 @@ __device__ __forceinline__ float fused_solve(const FusedParams& P, float sigma, 
   return m;
 }
 
+// Patch sums from the 12 limbs of an output voxel, then its clipped measure.
+__device__ __forceinline__ float fused_measure(const FusedParams& P, float sg, int s_u,
+                                               const int* L) {
+  long long Sx[5];
+#pragma unroll
+  for (int i = 0; i < 5; ++i)
+    Sx[i] = (long long)L[3 + 2 * i] * (1LL << P.kbits) + (long long)L[2 + 2 * i];
+  return fused_solve(P, sg, s_u, L[0], L[1], Sx[0], Sx[1], Sx[2], Sx[3], Sx[4]);
+}
+
 // Sobel magnitude at plane index c (centre of a 3x3 in-plane neighbourhood).
 template <int ND, int PW>
 __device__ __forceinline__ float fused_sobel(const float* mc, const float* S, const float* D,
@@ -243,6 +255,7 @@ template <int WND, typename TM, typename TS, int TY, int R>
 __device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
                                                    const TS* __restrict__ Ust,
                                                    const float* __restrict__ sig,
+                                                   const int* __restrict__ su,
                                                    const FusedParams& P, const Xform* X, int tile,
                                                    unsigned char* smem_raw, TileShared& T,
                                                    float* __restrict__ out_measure) {
@@ -299,17 +312,14 @@ __device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
   if (x < P.vx && y < P.vy) {
     const size_t gi = (size_t)y * P.vx + x;
     const float sg = __ldg(sig + gi);
+    const int sv = __ldg(su + gi);
     float m = 0.0f;
     if (sg > 0.0f) {
       const int* a = A + oy * G::HXP + ox;
       int L[kLimbs];
 #pragma unroll
       for (int k = 0; k < kLimbs; ++k) L[k] = a[k * PA];
-      long long Sx[5];
-#pragma unroll
-      for (int i = 0; i < 5; ++i)
-        Sx[i] = (long long)L[4 + 2 * i] * (1LL << P.kbits) + (long long)L[3 + 2 * i];
-      m = fused_solve(P, sg, L[0], L[1], L[2], Sx[0], Sx[1], Sx[2], Sx[3], Sx[4]);
+      m = fused_measure(P, sg, sv, L);
       acc_m = __float2int_rn(m * P.sum_scale);
     }
     if (out_measure) out_measure[gi] = m;
@@ -321,6 +331,7 @@ template <int ND, int WND, typename TM, typename TS, int TY, int R>
 __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* __restrict__ mov,
                                                       const TS* __restrict__ Ust,
                                                       const float* __restrict__ sig,
+                                                      const int* __restrict__ su,
                                                       FusedParams P,
                                                       const Xform* __restrict__ xf, int k0,
                                                       unsigned long long* __restrict__ acc,
@@ -374,22 +385,18 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
   }
 
   // solve one output voxel from the patch sums in A rows < TY
-  auto solve_out = [&](int z) {
+  // sg, sv: the voxel's weighting factor and static S_U, loaded a slice ahead
+  auto solve_out = [&](int z, float sg, int sv) {
     const int x = x0 + ox, y = y0 + oy;
     if (x < P.vx && y < P.vy) {
       const size_t gi = ((size_t)z * P.vy + y) * P.vx + x;
-      const float sg = __ldg(sig + gi);
       float m = 0.0f;
       if (sg > 0.0f) {
         const int* a = A + oy * G::HXP + ox;
         int L[kLimbs];
 #pragma unroll
         for (int k = 0; k < kLimbs; ++k) L[k] = a[k * PA];
-        long long Sx[5];
-#pragma unroll
-        for (int i = 0; i < 5; ++i)
-          Sx[i] = (long long)L[4 + 2 * i] * (1LL << P.kbits) + (long long)L[3 + 2 * i];
-        m = fused_solve(P, sg, L[0], L[1], L[2], Sx[0], Sx[1], Sx[2], Sx[3], Sx[4]);
+        m = fused_measure(P, sg, sv, L);
         acc_m += __float2int_rn(m * P.sum_scale);
       }
       if (out_measure && slot == 0) out_measure[gi] = m;
@@ -398,7 +405,7 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
 
   if constexpr (ND == 2) {
     __shared__ TileShared T;
-    acc_m = fused_tile_2d<WND, TM, TS, TY, R>(mov, Ust, sig, P, X, tile, smem_raw, T,
+    acc_m = fused_tile_2d<WND, TM, TS, TY, R>(mov, Ust, sig, su, P, X, tile, smem_raw, T,
                                               slot == 0 ? out_measure : nullptr);
   } else {
     // ---- 3D: z-marching over output slices [zb, ze) ----
@@ -439,6 +446,19 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
       }
     };
     load_u(e0);
+    // weighting factor and S_U of the output voxel of slice z, loaded one
+    // iteration before the solve that reads them
+    float sg_nx = 0.0f;
+    int sv_nx = 0;
+    auto load_sig = [&](int z) {
+      const int x = x0 + ox, y = y0 + oy;
+      if (z >= zb && z < ze && x < P.vx && y < P.vy) {
+        const size_t gi = ((size_t)z * P.vy + y) * P.vx + x;
+        sg_nx = __ldg(sig + gi);
+        sv_nx = __ldg(su + gi);
+      }
+    };
+    load_sig(e0 - R);
     auto warp_slice = [&](int zs, float* out) {
       const bool zin = (zs >= 0 && zs < P.vz);
 #pragma unroll
@@ -484,6 +504,8 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
       __syncthreads();
       set_base(e + 2);  // read by the next resample, after at least one barrier
       const int z = e - R;          // output slice completed by this entering slice
+      const float sg = sg_nx;
+      const int sv = sv_nx;
       const int l = e - 2 * R - 1;  // slice leaving the window
       const bool out = (z >= zb);
       const bool leave = (l >= e0);
@@ -518,10 +540,11 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
         }
       }
       load_u(e + 1);
+      load_sig(z + 1);
       __syncthreads();
       if (out) {
         fused_xy<ND, TY, R>(A);
-        solve_out(z);
+        solve_out(z, sg, sv);
       }
     }
   }
@@ -535,6 +558,7 @@ struct FusedLaunch {
   const void* mov;
   const void* ust;
   const float* sig;
+  const int* su;  // static window sum of the quantised ultrasound per voxel
   FusedParams P;
   const Xform* xf;
   int k0, cnt;
@@ -572,7 +596,7 @@ cudaError_t fused_launch_rt(const FusedLaunch& L) {
     P.zchunk = 1;
   }
   dim3 grid(L.cnt, ntx * nty, nz);
-  kern<<<grid, G::NT, G::BYTES, L.stream>>>((const T*)L.mov, (const T*)L.ust, L.sig, P, L.xf,
+  kern<<<grid, G::NT, G::BYTES, L.stream>>>((const T*)L.mov, (const T*)L.ust, L.sig, L.su, P, L.xf,
                                              L.k0, L.acc, L.out_measure);
   return cudaGetLastError();
 }

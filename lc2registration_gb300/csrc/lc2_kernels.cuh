@@ -628,4 +628,12 @@ __global__ void k_convert(const float* __restrict__ in, T* __restrict__ out, siz
   for (; i < n; i += step) out[i] = stf<T>(in[i]);
 }
 
+// Quantised static image qU = quant(U, qu), one int per voxel.
+template <typename TU>
+__global__ void k_quant_static(const TU* __restrict__ U, size_t n, float qu, int* __restrict__ out) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    out[i] = quant(ldf(U, i), qu);
+}
+
 }  // namespace lc2

@@ -20,6 +20,7 @@ struct ListSeg {
   const void* mov;    // moving image (storage type)
   const void* ust;    // static ultrasound on the virtual grid (storage type)
   const float* sig;   // weighting factor per virtual pixel
+  const int* su;      // static window sum of the quantised ultrasound per pixel
   FusedParams P;      // grid sizes and fixed-point scales; P.ntx = tiles along x
   int ntiles;         // tiles per evaluation
   int count;          // evaluations in the segment
@@ -59,7 +60,8 @@ __global__ void __launch_bounds__(32 * kListTY, 1)
     const int tile = (int)(rel - (long long)e * s_seg.ntiles);
     const int ev = s_seg.eval0 + e;
     long long m = fused_tile_2d<WND, T, T, kListTY, R>(
-        (const T*)s_seg.mov, (const T*)s_seg.ust, s_seg.sig, s_seg.P, xf + ev, tile, smem_raw, s_tile,
+        (const T*)s_seg.mov, (const T*)s_seg.ust, s_seg.sig, s_seg.su, s_seg.P, xf + ev, tile,
+        smem_raw, s_tile,
         nullptr);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m += __shfl_down_sync(0xffffffffu, m, o);
