@@ -301,7 +301,7 @@ def main():
     ctx = capi.Context(case.mode, case.fixed_geom, case.moving_geom, case.virt_spacing, case.r,
                        case.hr_moving, args.storage, device=local)
     ctx.set_images(case.fixed, case.moving)
-    tuned = ctx.autotune(mats[:64])  # tile height and z-chunk, timed on 64 transforms
+    tuned = ctx.autotune(mats[:64])  # tile height, kernel variant, z-chunk; timed on 64 transforms
     K = mats.shape[0]
     stream = torch.cuda.ExternalStream(ctx.stream())
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")

@@ -150,14 +150,21 @@ enum { LC2_OPTION_TILE_ROWS = 1 };
  * size; 0 issues the calls one by one. None of the options changes a
  * result: every sum is exact, whatever the tiling. */
 enum { LC2_OPTION_ZCHUNK = 2, LC2_OPTION_GRAPHS = 3 };
+/* LC2_OPTION_PIPELINE: 1 runs 3D evaluations with patch radius <= 4 on the
+ * warp-specialised fused kernel (producer warps resample the next slices
+ * into a shared ring while consumer warps do the moments); 0 (default) the
+ * single-role kernel. Same values either way. */
+enum { LC2_OPTION_PIPELINE = 4 };
 int lc2_set_option(lc2_context* ctx, int option, int value);
 
 /* CUDA-graph launches issued by lc2_evaluate_batch / lc2_evaluate. */
 long long lc2_graph_launches(const lc2_context* ctx);
 
 /* Autotuner: times the fused kernel on `count` transforms (matrices as in
- * lc2_evaluate_batch) for each tile height and z-chunk length it supports,
- * keeps the fastest as the context's options and returns them. Contexts
+ * lc2_evaluate_batch) for each tile height, kernel variant (single-role or
+ * warp-specialised, LC2_OPTION_PIPELINE) and z-chunk length it supports,
+ * keeps the fastest as the context's options and returns the tile height
+ * and z chunk. Contexts
  * without a tunable kernel (2D windows, HighResolutionModality: Fixed)
  * return their current settings. The reference takes fixed block sizes as
  * arguments (src/cu_LC2/cu_lc2_3d.cuh:36-41). */

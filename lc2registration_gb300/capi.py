@@ -28,6 +28,7 @@ MODES = {"2D": 0, "3D": 1, "2DTo3D": 2}
 OPTION_TILE_ROWS = 1
 OPTION_ZCHUNK = 2
 OPTION_GRAPHS = 3
+OPTION_PIPELINE = 4
 STORAGE = {"f32": 0, "f16": 1, "bf16": 2}
 
 # Every symbol include/lc2.h declares (checked by the test suite).

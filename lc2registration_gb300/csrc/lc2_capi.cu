@@ -99,6 +99,9 @@ struct lc2_context {
   double h_static = 0.0;
   int tile_rows = 0;  // fused kernel tile height (0 = automatic)
   int zchunk = 0;     // fused kernel output slices per CTA (0 = automatic)
+  int pipeline = 0;   // warp-specialised fused 3D kernel (LC2_OPTION_PIPELINE)
+  int* d_err = nullptr;   // device flag of the warp-specialised kernel's bounded waits
+  int* h_err = nullptr;   // pinned copy
 
   // CUDA graphs of lc2_evaluate_batch's sequence (copy-in, fused launch,
   // ratio, copy-out) by batch size; dropped when buffers or options change
@@ -462,6 +465,8 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
   L.wnd = c->warp_nd;
   L.tile_height = c->tile_rows > 0 ? c->tile_rows : 16;
   L.zchunk = c->zchunk;
+  L.pipeline = c->pipeline;
+  L.err = c->d_err;
   L.stream = c->stream;
   cudaError_t e;
   {
@@ -537,6 +542,15 @@ int launch_finalize(lc2_context* c, int count) {
 
 int matrix_floats(const lc2_context* c) { return c->warp_nd == 2 ? 9 : 16; }
 
+// A wait of the warp-specialised kernel ran past its deadline (the flag is
+// copied to h_err with the results): the values of that launch are invalid.
+int check_pipeline(lc2_context* c) {
+  if (*c->h_err == 0) return LC2_OK;
+  *c->h_err = 0;
+  cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+  return fail(LC2_ERR_CUDA, "pipelined kernel: a producer/consumer wait timed out");
+}
+
 int check_ctx(const lc2_context* c) {
   if (!c) return fail(LC2_ERR_INVALID_ARGUMENT, "null context");
   if (!c->ready) return fail(LC2_ERR_NOT_READY, "images not set (call lc2_set_images first)");
@@ -604,6 +618,8 @@ int plan_context(const lc2_config* cfg, lc2_context* c) {
   c->nv = (size_t)c->virt.dim[0] * c->virt.dim[1] * c->virt.dim[2];
   c->nf = (size_t)c->cfg.fixed.dim[0] * c->cfg.fixed.dim[1] * c->cfg.fixed.dim[2];
   c->nm = (size_t)c->cfg.moving.dim[0] * c->cfg.moving.dim[1] * c->cfg.moving.dim[2];
+  if (c->nm >= (size_t)1 << 31 || c->nf >= (size_t)1 << 31)
+    return fail(LC2_ERR_UNSUPPORTED, "images are limited to 2^31 - 1 voxels (32-bit gather indices)");
   c->n = (2 * r + 1) * (2 * r + 1) * (c->lc2_nd == 3 ? (2 * r + 1) : 1);
   // fixed-point bits: n * 2^(b+1) <= 2^31 (int32 first-order sums with one
   // bit of headroom; then n^2 2^(2b) <= 2^60 for the centred int64 sums)
@@ -671,6 +687,9 @@ int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
   if (e == cudaSuccess && cfg->high_res_is_moving && !c->mi)
     e = cudaMalloc(&c->d_su, c->nv * sizeof(int));
   if (e == cudaSuccess && c->mi) e = cudaMalloc(&c->d_sbin, c->nv);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMallocHost(&c->h_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(int));
   if (e != cudaSuccess) {
     lc2_destroy(c);
     return fail(LC2_ERR_OUT_OF_MEMORY, "device allocation: %s", cudaGetErrorString(e));
@@ -715,6 +734,8 @@ int lc2_destroy(lc2_context* c) {
   cudaFree(c->d_gstatic);
   cudaFree(c->d_sigma);
   cudaFree(c->d_su);
+  cudaFree(c->d_err);
+  if (c->h_err) cudaFreeHost(c->h_err);
   cudaFree(c->d_scratch);
   drop_graphs(c);
   cudaFree(c->d_sbin);
@@ -771,6 +792,11 @@ int lc2_set_option(lc2_context* c, int option, int value) {
   if (option == LC2_OPTION_ZCHUNK) {
     if (value < 0) return fail(LC2_ERR_INVALID_ARGUMENT, "z chunk must be >= 0");
     c->zchunk = value;
+    drop_graphs(c);
+    return LC2_OK;
+  }
+  if (option == LC2_OPTION_PIPELINE) {
+    c->pipeline = value != 0;
     drop_graphs(c);
     return LC2_OK;
   }
@@ -1062,6 +1088,7 @@ int enqueue_batch(lc2_context* c, int count) {
   }
   LC2_CUDA(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(double) * count, cudaMemcpyDeviceToHost,
                            c->stream));
+  LC2_CUDA(cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   return LC2_OK;
 }
 
@@ -1146,7 +1173,9 @@ int lc2_fetch_results(lc2_context* c, double* out, int count) {
   if (count > 0)
     LC2_CUDA(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(double) * count, cudaMemcpyDeviceToHost,
                              c->stream));
+  LC2_CUDA(cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   LC2_CUDA(cudaStreamSynchronize(c->stream));
+  LC2_TRY(check_pipeline(c));
   if (count > 0) std::memcpy(out, c->h_out, sizeof(double) * count);
   return LC2_OK;
 }
@@ -1161,6 +1190,7 @@ int lc2_evaluate_batch(lc2_context* c, const float* matrices, int count, double*
     c->staged = count;
     LC2_TRY(launch_batch_graph(c, count));
     LC2_CUDA(cudaStreamSynchronize(c->stream));
+    LC2_TRY(check_pipeline(c));
     std::memcpy(out, c->h_out, sizeof(double) * count);
     return LC2_OK;
   }
@@ -1764,11 +1794,19 @@ extern "C" int lc2_autotune(lc2_context* c, const float* matrices, int count, in
     const bool timing = c->timing;
     c->timing = false;
     float best = 0.0f;
-    int best_rows = rows[0], best_chunk = 0;
+    int best_rows = rows[0], best_chunk = 0, best_pipe = 0;
     int st = LC2_OK;
-    for (int tr : rows) {
+    struct Cand {
+      int rows, pipeline;
+    };
+    std::vector<Cand> cands;
+    for (int tr : rows) cands.push_back({tr, 0});
+    if (r <= 4) cands.push_back({16, 1});
+    for (const Cand& cd : cands) {
+      const int tr = cd.rows;
       for (int zc : chunks) {
         c->tile_rows = tr;
+        c->pipeline = cd.pipeline;
         c->zchunk = zc;
         float ms = 0.0f;
         for (int rep = 0; rep < 2 && st == LC2_OK; ++rep) {  // warm-up, then timed
@@ -1788,6 +1826,7 @@ extern "C" int lc2_autotune(lc2_context* c, const float* matrices, int count, in
           best = ms;
           best_rows = tr;
           best_chunk = zc;
+          best_pipe = cd.pipeline;
         }
       }
       if (st != LC2_OK) break;
@@ -1795,7 +1834,12 @@ extern "C" int lc2_autotune(lc2_context* c, const float* matrices, int count, in
     c->timing = timing;
     c->tile_rows = best_rows;
     c->zchunk = best_chunk;
+    c->pipeline = best_pipe;
     drop_graphs(c);
+    if (st == LC2_OK) {
+      LC2_CUDA(cudaMemcpy(c->h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+      st = check_pipeline(c);
+    }
     if (st != LC2_OK) return st;
   }
   if (tile_rows) *tile_rows = c->tile_rows > 0 ? c->tile_rows : 16;

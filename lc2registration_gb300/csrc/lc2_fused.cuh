@@ -87,23 +87,56 @@ __device__ __forceinline__ float fused_sample(const TM* __restrict__ mov, const 
     float qz = fmaf(A[7], dy, fmaf(A[6], dx, sf[2]));
     Axis az = make_axis(sb[2], qz, P.mz);
     if (!(ax.ok && ay.ok && az.ok)) return 0.0f;
-    const size_t sy = (size_t)P.mx, szs = (size_t)P.mx * P.my;
-    const size_t zf = az.f * szs, zc = az.c * szs, yf = ay.f * sy, yc = ay.c * sy;
-    float lu0 = ldf(mov, ax.f + yf + zf), lu1 = ldf(mov, ax.f + yf + zc);
-    float ru0 = ldf(mov, ax.c + yf + zf), ru1 = ldf(mov, ax.c + yf + zc);
-    float rb0 = ldf(mov, ax.c + yc + zf), rb1 = ldf(mov, ax.c + yc + zc);
-    float lb0 = ldf(mov, ax.f + yc + zf), lb1 = ldf(mov, ax.f + yc + zc);
+    // one 32-bit linear index and the corner offsets (volumes hold < 2^31
+    // voxels, checked on the host)
+    const unsigned mxy = (unsigned)P.mx * (unsigned)P.my;
+    const unsigned b = (unsigned)ax.f + (unsigned)ay.f * (unsigned)P.mx + (unsigned)az.f * mxy;
+    const unsigned ox = (unsigned)(ax.c - ax.f), oy = (unsigned)(ay.c - ay.f) * (unsigned)P.mx,
+                   oz = (unsigned)(az.c - az.f) * mxy;
+    float lu0 = ldf(mov, b), lu1 = ldf(mov, b + oz);
+    float ru0 = ldf(mov, b + ox), ru1 = ldf(mov, b + ox + oz);
+    float rb0 = ldf(mov, b + ox + oy), rb1 = ldf(mov, b + ox + oy + oz);
+    float lb0 = ldf(mov, b + oy), lb1 = ldf(mov, b + oy + oz);
     float lu = fmaf(az.r, lu1 - lu0, lu0), ru = fmaf(az.r, ru1 - ru0, ru0);
     float rb = fmaf(az.r, rb1 - rb0, rb0), lb = fmaf(az.r, lb1 - lb0, lb0);
     float l = fmaf(ay.r, lb - lu, lu), r = fmaf(ay.r, rb - ru, ru);
     return fmaf(ax.r, r - l, l);
   }
   if (!(ax.ok && ay.ok)) return 0.0f;
-  const size_t yf = (size_t)ay.f * P.mx, yc = (size_t)ay.c * P.mx;
-  float f0 = ldf(mov, ax.f + yf), f1 = ldf(mov, ax.f + yc);
-  float c0 = ldf(mov, ax.c + yf), c1 = ldf(mov, ax.c + yc);
+  const unsigned b = (unsigned)ax.f + (unsigned)ay.f * (unsigned)P.mx;
+  const unsigned ox = (unsigned)(ax.c - ax.f), oy = (unsigned)(ay.c - ay.f) * (unsigned)P.mx;
+  float f0 = ldf(mov, b), f1 = ldf(mov, b + oy);
+  float c0 = ldf(mov, b + ox), c1 = ldf(mov, b + ox + oy);
   float xl = fmaf(ay.r, f1 - f0, f0), xr = fmaf(ay.r, c1 - c0, c0);
   return fmaf(ax.r, xr - xl, xl);
+}
+
+// Trilinear sample of a point known to lie strictly inside the moving volume
+// (the region test of set_base): no bounds tests, corner offsets fixed. The
+// ceil corner is always floor + 1; where the fraction is 0 its weight is 0,
+// so the value equals fused_sample's bit for bit.
+template <typename TM>
+__device__ __forceinline__ float fused_sample_inside(const TM* __restrict__ mov,
+                                                     const FusedParams& P, const float* A,
+                                                     const int* sb, const float* sf, int px,
+                                                     int py) {
+  const float dx = (float)px, dy = (float)py;
+  const float qx = fmaf(A[1], dy, fmaf(A[0], dx, sf[0]));
+  const float qy = fmaf(A[4], dy, fmaf(A[3], dx, sf[1]));
+  const float qz = fmaf(A[7], dy, fmaf(A[6], dx, sf[2]));
+  const float flx = floorf(qx), fly = floorf(qy), flz = floorf(qz);
+  const float rx = qx - flx, ry = qy - fly, rz = qz - flz;
+  const unsigned mx = (unsigned)P.mx, mxy = (unsigned)P.mx * (unsigned)P.my;
+  const unsigned b = (unsigned)(sb[0] + (int)flx) + (unsigned)(sb[1] + (int)fly) * mx +
+                     (unsigned)(sb[2] + (int)flz) * mxy;
+  float lu0 = ldf(mov, b), lu1 = ldf(mov, b + mxy);
+  float ru0 = ldf(mov, b + 1), ru1 = ldf(mov, b + 1 + mxy);
+  float rb0 = ldf(mov, b + 1 + mx), rb1 = ldf(mov, b + 1 + mx + mxy);
+  float lb0 = ldf(mov, b + mx), lb1 = ldf(mov, b + mx + mxy);
+  float lu = fmaf(rz, lu1 - lu0, lu0), ru = fmaf(rz, ru1 - ru0, ru0);
+  float rb = fmaf(rz, rb1 - rb0, rb0), lb = fmaf(rz, lb1 - lb0, lb0);
+  float l = fmaf(ry, lb - lu, lu), r = fmaf(ry, rb - ru, ru);
+  return fmaf(rx, r - l, l);
 }
 
 // 12 limbs of one point's moment fields: qM, qG, then (lo, hi) of the
@@ -126,7 +159,18 @@ __device__ __forceinline__ void fused_limbs(int qu, int qm, int qg, int K, int* 
 // < TY, columns < 32 hold the patch sums. One thread per (limb, row), then
 // per (limb, column); each loads its whole row or column into registers
 // before writing, so the passes need no second buffer.
-template <int ND, int TY, int R>
+// Barrier of the threads that run the window passes: the whole CTA (BAR = 0)
+// or, in the warp-specialised kernel, named barrier BAR of its NT threads.
+template <int BAR, int NT>
+__device__ __forceinline__ void group_sync() {
+  if constexpr (BAR == 0) {
+    __syncthreads();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"n"(BAR), "n"(NT) : "memory");
+  }
+}
+
+template <int ND, int TY, int R, int BAR = 0>
 __device__ __forceinline__ void fused_xy(int* __restrict__ A) {
   using G = FusedGeom<ND, TY, R>;
   const int tid = threadIdx.x;
@@ -145,7 +189,7 @@ __device__ __forceinline__ void fused_xy(int* __restrict__ A) {
       row[x] = a;
     }
   }
-  __syncthreads();
+  group_sync<BAR, G::NT>();
   for (int it = tid; it < kLimbs * 32; it += G::NT) {
     const int L = it >> 5, col = it & 31;
     int* c = A + (size_t)L * G::HY * G::HXP + col;
@@ -162,7 +206,7 @@ __device__ __forceinline__ void fused_xy(int* __restrict__ A) {
       c[y * G::HXP] = a;
     }
   }
-  __syncthreads();
+  group_sync<BAR, G::NT>();
 }
 
 // Clipped measure of one voxel from exact sums; sigma > 0 is the
@@ -349,6 +393,7 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
   __shared__ int s_ib[3];
   __shared__ float s_fb[3];
   __shared__ float s_A[9];
+  __shared__ int s_inside;  // the region of the current slice samples strictly inside
   const int tid = threadIdx.x;
   const int slot = blockIdx.x;
   const int tile = blockIdx.y;
@@ -367,13 +412,25 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
   // and fraction for the float per-point offsets
   auto set_base = [&](int zs) {
     if (tid == 0) {
+      // the region lies in the virtual grid and every sample of it strictly
+      // inside the moving volume (0 <= floor, floor + 1 <= dim - 1; corners of
+      // the region bound the affine image, 0.01 voxel covers float rounding)
+      bool in = ND == 3 && zs >= 0 && zs < P.vz && gx0 >= 0 && gx0 + G::PW <= P.vx &&
+                gy0 >= 0 && gy0 + G::PH <= P.vy;
+      const int dims[3] = {P.mx, P.my, P.mz};
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
         double p = s_base[a] + X->A[3 * a + 2] * (double)zs;
         double fl = floor(p);
         s_ib[a] = (int)fl;
         s_fb[a] = (float)(p - fl);
+        const float ex = s_A[3 * a] * (float)(G::PW - 1);
+        const float e0 = s_A[3 * a + 1] * (float)yb, e1 = s_A[3 * a + 1] * (float)(yb + G::PH - 1);
+        const float lo = s_fb[a] + fminf(ex, 0.0f) + fminf(e0, e1);
+        const float hi = s_fb[a] + fmaxf(ex, 0.0f) + fmaxf(e0, e1);
+        in = in && ((float)s_ib[a] + lo >= 0.01f) && ((float)s_ib[a] + hi <= (float)(dims[a] - 1) - 0.01f);
       }
+      s_inside = in ? 1 : 0;
     }
   };
   if (tid == 0) {
@@ -461,6 +518,19 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
     load_sig(e0 - R);
     auto warp_slice = [&](int zs, float* out) {
       const bool zin = (zs >= 0 && zs < P.vz);
+      if (s_inside) {
+#pragma unroll
+        for (int k = 0; k < WP; ++k) {
+          const int i = tid + k * NT;
+          float v = 0.0f;
+          if (i < G::NPW) {
+            const int py = i / G::PW, px = i - py * G::PW;
+            v = fused_sample_inside<TM>(mov, P, s_A, s_ib, s_fb, px, py + yb);
+          }
+          out[k] = v;
+        }
+        return;
+      }
 #pragma unroll
       for (int k = 0; k < WP; ++k) {
         const int i = tid + k * NT;
@@ -567,6 +637,8 @@ struct FusedLaunch {
   int nd, wnd;
   int tile_height;  // 3D, radius <= 4: 16 or 8 rows per tile
   int zchunk;       // 3D: output slices per CTA; 0 = automatic
+  int pipeline;     // 3D, radius <= 4, no per-voxel output: warp-specialised kernel
+  int* err;         // device flag raised by the warp-specialised kernel's bounded waits
   cudaStream_t stream;
 };
 
@@ -643,6 +715,11 @@ cudaError_t fused_launch_nd(const FusedLaunch& L) {
   return cudaErrorInvalidValue;
 }
 
+// Warp-specialised 3D kernel (lc2_fused_ws.cuh), defined in the same
+// translation units.
+template <typename T>
+cudaError_t fused_ws_launch(const FusedLaunch& L, int* err);
+
 template <>
 cudaError_t fused_launch<float>(const FusedLaunch& L);
 template <>
@@ -653,6 +730,8 @@ cudaError_t fused_launch<__nv_bfloat16>(const FusedLaunch& L);
 #define LC2_DEFINE_FUSED_LAUNCH(T)                                  \
   template <>                                                       \
   cudaError_t fused_launch<T>(const FusedLaunch& L) {               \
+    if (L.nd == 3 && L.pipeline && L.P.r <= 4 && !L.out_measure)    \
+      return fused_ws_launch<T>(L, L.err);                          \
     if (L.nd == 3) return fused_launch_nd<3, 3, T>(L);              \
     if (L.wnd == 3) return fused_launch_nd<2, 3, T>(L);             \
     return fused_launch_nd<2, 2, T>(L);                             \

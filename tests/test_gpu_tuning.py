@@ -74,3 +74,16 @@ def test_2d_context_graphs():
     np.testing.assert_array_equal(got, _staged(ctx, mats))
     np.testing.assert_array_equal([ctx.evaluate(m) for m in mats], got)
     assert ctx.autotune(mats) == (16, 0)
+
+
+@pytest.mark.parametrize("r", [1, 2, 4])
+def test_warp_specialised_kernel_equals_single_role(r):
+    case = synth.case_3d(seed=24 + r, mr_size=48, us_size=40, r=r, blobs=6)
+    ctx = make_context(case, "f16")
+    mats = perturbed(case, np.random.default_rng(5), 9)
+    ref = ctx.evaluate_batch(mats)
+    ctx.set_option(capi.OPTION_PIPELINE, 1)
+    for zc in (0, 9, 40):
+        ctx.set_option(capi.OPTION_ZCHUNK, zc)
+        np.testing.assert_array_equal(ctx.evaluate_batch(mats), ref)
+        np.testing.assert_array_equal(_staged(ctx, mats), ref)
