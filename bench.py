@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch options")
     ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--serve-rate", type=float, default=4.0, help="Poisson arrivals per second")
     ap.add_argument("--serve-active", type=int, default=8)
@@ -301,7 +302,8 @@ def main():
     ctx = capi.Context(case.mode, case.fixed_geom, case.moving_geom, case.virt_spacing, case.r,
                        case.hr_moving, args.storage, device=local)
     ctx.set_images(case.fixed, case.moving)
-    tuned = ctx.autotune(mats[:64])  # tile height, kernel variant, z-chunk; timed on 64 transforms
+    # tile height, kernel variant, z-chunk; timed on 64 transforms
+    tuned = (16, 0) if args.no_autotune else ctx.autotune(mats[:64])
     K = mats.shape[0]
     stream = torch.cuda.ExternalStream(ctx.stream())
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")

@@ -52,16 +52,22 @@ struct FusedGeom {
   static constexpr int NT = 32 * TY;
   static constexpr int PW = 32 + 2 * R + 2, PH = TY + 2 * R + 2;  // resampled region
   static constexpr int HX = 32 + 2 * R, HY = TY + 2 * R;          // patch halo region
-  static constexpr int HXP = HX | 1, TXP = 33;                    // plane pitches
+  // limb-plane row pitch: 4 x an odd number of words, so rows are 16-byte
+  // aligned and eight threads reading eight rows with 128-bit loads hit
+  // distinct bank groups
+  static constexpr int HXP = (((HX + 3) / 4) | 1) * 4, TXP = 33;
   static constexpr int W = 2 * R + 1;
   static constexpr int NP = HX * HY, NPW = PW * PH;
   static constexpr int RING = (ND == 3) ? 2 * R + 2 : 0;
   static constexpr int MAXP = (NP + NT - 1) / NT;   // halo points per thread
   static constexpr int WP = (NPW + NT - 1) / NT;    // resampled points per thread
   static constexpr int NPLANES = (ND == 3) ? 3 : 1;
-  // shared memory: M / Sz / Dz planes, leaving ring, limb planes
+  // leaving ring entries per point: qM, qG, and qU where shared memory allows
+  // (16-row tiles run one CTA per SM; 8-row tiles keep two CTAs resident)
+  static constexpr int RINGW = (ND == 3 && TY == 16) ? 3 : 2;
+  // shared memory: M plane, interleaved (Sz, Dz) plane, leaving ring, limb planes
   static constexpr size_t OFF_LV = sizeof(float) * (size_t)NPLANES * NPW;
-  static constexpr size_t OFF_A = OFF_LV + sizeof(int) * (size_t)RING * 2 * NP;
+  static constexpr size_t OFF_A = OFF_LV + sizeof(int) * (size_t)RING * RINGW * NP;
   static constexpr size_t BYTES = OFF_A + sizeof(int) * (size_t)kLimbs * HY * HXP;
 };
 
@@ -176,17 +182,26 @@ __device__ __forceinline__ void fused_xy(int* __restrict__ A) {
   const int tid = threadIdx.x;
   for (int it = tid; it < kLimbs * G::HY; it += G::NT) {
     int* row = A + (size_t)it * G::HXP;  // it = limb * HY + row
-    int v[G::HX];
+    constexpr int NV = (G::HX + 3) / 4;   // 128-bit loads covering the row
+    int v[4 * NV];
 #pragma unroll
-    for (int i = 0; i < G::HX; ++i) v[i] = row[i];
+    for (int i = 0; i < NV; ++i) {
+      const int4 q = reinterpret_cast<const int4*>(row)[i];
+      v[4 * i] = q.x;
+      v[4 * i + 1] = q.y;
+      v[4 * i + 2] = q.z;
+      v[4 * i + 3] = q.w;
+    }
     int a = 0;
 #pragma unroll
     for (int i = 0; i < G::W; ++i) a += v[i];
-    row[0] = a;
+    int o[4];
+    o[0] = a;
 #pragma unroll
     for (int x = 1; x < 32; ++x) {
       a += v[x + G::W - 1] - v[x - 1];
-      row[x] = a;
+      o[x & 3] = a;
+      if ((x & 3) == 3) reinterpret_cast<int4*>(row)[x >> 2] = make_int4(o[0], o[1], o[2], o[3]);
     }
   }
   group_sync<BAR, G::NT>();
@@ -280,6 +295,22 @@ __device__ __forceinline__ float fused_sobel(const float* mc, const float* S, co
   float gx = (M[up + 1] - M[up - 1]) + 2.0f * (M[c + 1] - M[c - 1]) + (M[dn + 1] - M[dn - 1]);
   float gy = (M[dn - 1] - M[up - 1]) + 2.0f * (M[dn] - M[up]) + (M[dn + 1] - M[up + 1]);
   return sqrtf(gx * gx + gy * gy);
+}
+
+// 3D Sobel magnitude at plane index c from the interleaved (Sz, Dz) plane:
+// the nine 64-bit reads of the 3x3 neighbourhood, same arithmetic as
+// fused_sobel<3>.
+template <int PW>
+__device__ __forceinline__ float fused_sobel_sd(const float2* SD, int c) {
+  const int up = c - PW, dn = c + PW;
+  const float2 a0 = SD[up - 1], a1 = SD[up], a2 = SD[up + 1];
+  const float2 b0 = SD[c - 1], b1 = SD[c], b2 = SD[c + 1];
+  const float2 c0 = SD[dn - 1], c1 = SD[dn], c2 = SD[dn + 1];
+  float gx = (a2.x - a0.x) + 2.0f * (b2.x - b0.x) + (c2.x - c0.x);
+  float gy = (c0.x - a0.x) + 2.0f * (c1.x - a1.x) + (c2.x - a2.x);
+  float gz = (a0.y + 2.0f * a1.y + a2.y) + 2.0f * (b0.y + 2.0f * b1.y + b2.y) +
+             (c0.y + 2.0f * c1.y + c2.y);
+  return sqrtf(gx * gx + gy * gy + gz * gz);
 }
 
 // Per-tile transform state in shared memory.
@@ -384,8 +415,7 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
   constexpr int NT = G::NT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* mc = reinterpret_cast<float*>(smem_raw);
-  float* S = mc + G::NPW;
-  float* D = mc + 2 * G::NPW;
+  float2* SD = reinterpret_cast<float2*>(mc + G::NPW);  // NPW is even: 8-byte aligned
   int* lv = reinterpret_cast<int*>(smem_raw + G::OFF_LV);
   int* A = reinterpret_cast<int*>(smem_raw + G::OFF_A);
   constexpr size_t PA = (size_t)G::HY * G::HXP;
@@ -499,7 +529,10 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
 #pragma unroll
       for (int j = 0; j < MAXP; ++j) {
         u_in[j] = (pin[j] && ezin) ? ldf(Ust, (size_t)e * slice + pu[j]) : 0.0f;
-        u_out[j] = (pin[j] && lzin) ? ldf(Ust, (size_t)l * slice + pu[j]) : 0.0f;
+        if constexpr (G::RINGW == 2)
+          u_out[j] = (pin[j] && lzin) ? ldf(Ust, (size_t)l * slice + pu[j]) : 0.0f;
+        else
+          u_out[j] = 0.0f;  // the ring holds the leaving qU
       }
     };
     load_u(e0);
@@ -564,8 +597,7 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
           const int i = tid + k * NT;
           if (i < G::NPW) {
             mc[i] = m_prev1[k];
-            S[i] = m_prev2[k] + 2.0f * m_prev1[k] + m_next[k];
-            D[i] = m_next[k] - m_prev2[k];
+            SD[i] = make_float2(m_prev2[k] + 2.0f * m_prev1[k] + m_next[k], m_next[k] - m_prev2[k]);
           }
           m_prev2[k] = m_prev1[k];
           m_prev1[k] = m_next[k];
@@ -579,23 +611,24 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
       const int l = e - 2 * R - 1;  // slice leaving the window
       const bool out = (z >= zb);
       const bool leave = (l >= e0);
-      int* lv_in = lv + ((e - e0) % G::RING) * 2 * G::NP;
-      const int* lv_out = lv + ((l - e0 + G::RING) % G::RING) * 2 * G::NP;
+      int* lv_in = lv + ((e - e0) % G::RING) * G::RINGW * G::NP;
+      const int* lv_out = lv + ((l - e0 + G::RING) % G::RING) * G::RINGW * G::NP;
 #pragma unroll
       for (int j = 0; j < MAXP; ++j) {
         const int p = tid + j * NT;
         if (p < G::NP) {
-          const float u = u_in[j], ul = u_out[j];
           const float m = mc[pc[j]];
-          const float g = fused_sobel<3, G::PW>(mc, S, D, pc[j]);
-          const int qm = quant(m, P.qm), qg = quant(g, P.qg);
+          const float g = fused_sobel_sd<G::PW>(SD, pc[j]);
+          const int qm = quant(m, P.qm), qg = quant(g, P.qg), qu = quant(u_in[j], P.qu);
           int Li[kLimbs];
-          fused_limbs(quant(u, P.qu), qm, qg, P.kbits, Li);
+          fused_limbs(qu, qm, qg, P.kbits, Li);
           lv_in[p] = qm;
           lv_in[G::NP + p] = qg;
+          if constexpr (G::RINGW == 3) lv_in[2 * G::NP + p] = qu;
           if (leave) {
             int Lo[kLimbs];
-            fused_limbs(quant(ul, P.qu), lv_out[p], lv_out[G::NP + p], P.kbits, Lo);
+            const int qul = (G::RINGW == 3) ? lv_out[2 * G::NP + p] : quant(u_out[j], P.qu);
+            fused_limbs(qul, lv_out[p], lv_out[G::NP + p], P.kbits, Lo);
 #pragma unroll
             for (int k = 0; k < kLimbs; ++k) acc32[j][k] += Li[k] - Lo[k];
           } else {

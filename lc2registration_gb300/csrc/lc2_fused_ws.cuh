@@ -80,9 +80,8 @@ template <int R>
 struct WsGeom {
   using G = FusedGeom<3, 16, R>;
   static constexpr int NT = G::NT + kWsProducers;  // 640
-  static constexpr size_t OFF_S = sizeof(float) * (size_t)kWsSlots * G::NPW;
-  static constexpr size_t OFF_D = OFF_S + sizeof(float) * (size_t)G::NPW;
-  static constexpr size_t OFF_LV = OFF_D + sizeof(float) * (size_t)G::NPW;
+  static constexpr size_t OFF_SD = sizeof(float) * (size_t)kWsSlots * G::NPW;
+  static constexpr size_t OFF_LV = OFF_SD + sizeof(float2) * (size_t)G::NPW;
   static constexpr size_t OFF_A = OFF_LV + sizeof(int) * (size_t)G::RING * 2 * G::NP;
   static constexpr size_t BYTES = OFF_A + sizeof(int) * (size_t)kLimbs * G::HY * G::HXP;
 };
@@ -100,8 +99,7 @@ __global__ void __launch_bounds__(WsGeom<R>::NT, 1)
   constexpr size_t PA = (size_t)G::HY * G::HXP;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* ring = reinterpret_cast<float*>(smem_raw);
-  float* S = reinterpret_cast<float*>(smem_raw + W::OFF_S);
-  float* D = reinterpret_cast<float*>(smem_raw + W::OFF_D);
+  float2* SD = reinterpret_cast<float2*>(smem_raw + W::OFF_SD);
   int* lv = reinterpret_cast<int*>(smem_raw + W::OFF_LV);
   int* A = reinterpret_cast<int*>(smem_raw + W::OFF_A);
   __shared__ __align__(8) unsigned long long full[kWsSlots], empty[kWsSlots];
@@ -235,8 +233,7 @@ __global__ void __launch_bounds__(WsGeom<R>::NT, 1)
     const float* Mn = ring + (size_t)(qn % kWsSlots) * G::NPW;        // slice e + 1
     for (int i = tid; i < G::NPW; i += NC) {
       const float a = Mp[i], b = Mc[i], c = Mn[i];
-      S[i] = a + 2.0f * b + c;
-      D[i] = c - a;
+      SD[i] = make_float2(a + 2.0f * b + c, c - a);
     }
     group_sync<1, NC>();
     if (tid == 0) mbar_arrive(&empty[(qn - 2) % kWsSlots]);  // slice e - 1 is no longer read
@@ -254,7 +251,7 @@ __global__ void __launch_bounds__(WsGeom<R>::NT, 1)
       if (p < G::NP) {
         const float u = u_in[j], ul = u_out[j];
         const float m = Mc[pc[j]];
-        const float g = fused_sobel<3, G::PW>(Mc, S, D, pc[j]);
+        const float g = fused_sobel_sd<G::PW>(SD, pc[j]);
         const int qm = quant(m, P.qm), qg = quant(g, P.qg);
         int Li[kLimbs];
         fused_limbs(quant(u, P.qu), qm, qg, P.kbits, Li);
