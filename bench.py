@@ -245,6 +245,21 @@ def serve_leg(args, main_case, device):
     }
 
 
+def replica_rate(units_local: float, seconds_local: float, dist=None, device=None) -> float:
+    """Whole-job throughput of independent replicas: the units of every rank
+    over the slowest rank's time (max over ranks, as the driver measures)."""
+    if dist is None:
+        return units_local / seconds_local
+    import torch
+
+    t = torch.tensor([seconds_local, units_local], dtype=torch.float64, device=device)
+    tmax = t[:1].clone()
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    units = t[1:].clone()
+    dist.all_reduce(units, op=dist.ReduceOp.SUM)
+    return float(units.item()) / float(tmax.item())
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -335,11 +350,8 @@ def main():
     launches = ctx.launch_count() - launches0
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(step_ms)
-    if dist:
-        t = torch.tensor([total_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * K * args.steps / (total_ms / 1e3)
+    value = replica_rate(K * args.steps, total_ms / 1e3, dist, f"cuda:{local}")
+    total_ms = world * K * args.steps / value * 1e3  # the slowest rank's time
     res = ctx.fetch(K)
     assert np.all(np.isfinite(res)) and res.max() > 0
 
@@ -377,11 +389,7 @@ def main():
         t0 = time.perf_counter()
         out = ctx.evaluate_batch(mats)
         e2e_t += time.perf_counter() - t0
-    e2e = world * K * args.steps / e2e_t if world == 1 else None
-    if dist:
-        t = torch.tensor([e2e_t], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e = world * K * args.steps / float(t.item())
+    e2e = replica_rate(K * args.steps, e2e_t, dist, f"cuda:{local}")
     assert np.array_equal(out, res), "batched results changed between runs"
 
     # ---- plain form: one evaluation per call ----
