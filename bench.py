@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="default launch options")
+    ap.add_argument("--no-small", action="store_true", help="skip the 2D 256^2 / 3D 96^3 lines")
     ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--serve-rate", type=float, default=4.0, help="Poisson arrivals per second")
     ap.add_argument("--serve-active", type=int, default=8)
@@ -260,6 +261,51 @@ def replica_rate(units_local: float, seconds_local: float, dist=None, device=Non
     return float(units.item()) / float(tmax.item())
 
 
+def small_configs(device):
+    """Batched vs plain on the small configurations (2D 256^2, 7x7 patches;
+    3D 128^3 -> 96^3, 7^3 patches), where one evaluation does not fill the
+    GPU: device-timed batches of 512 and 256 transforms, and one
+    lc2_evaluate per transform through the public call (host in / host out)."""
+    import numpy as np
+    import torch
+
+    from lc2registration_gb300 import capi, synth
+    from tests.helpers import perturbed
+
+    out = {}
+    for name, case, K in (("2d_256_r3", synth.case_2d(seed=7, size=256, r=3), 512),
+                          ("3d_128_96_r3", synth.case_3d(seed=8, mr_size=128, us_size=96, r=3), 256)):
+        ctx = capi.Context(case.mode, case.fixed_geom, case.moving_geom, case.virt_spacing, case.r,
+                           True, "f32", device=device)
+        ctx.set_images(case.fixed, case.moving)
+        mats = perturbed(case, np.random.default_rng(3), K)
+        ctx.stage(mats)
+        stream = torch.cuda.ExternalStream(ctx.stream())
+        for _ in range(3):
+            ctx.launch(K)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for _ in range(5):
+            ctx.launch(K)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        batched = 5 * K / (ev[0].elapsed_time(ev[1]) / 1e3)
+        vals = ctx.fetch(K)
+        for m in mats[:8]:
+            ctx.evaluate(m)
+        n = 200
+        t0 = time.perf_counter()
+        plain = [ctx.evaluate(m) for m in mats[:n % K or K][:n]]
+        plain_eps = len(plain) / (time.perf_counter() - t0)
+        assert np.array_equal(np.array(plain), vals[:len(plain)]), "plain != batched"
+        out[name] = {"batched_evals_per_s": batched, "plain_evals_per_s": plain_eps,
+                     "batched_over_plain": batched / plain_eps, "candidates_per_launch": K,
+                     "virtual_voxels": int(np.prod(ctx.virtual_dims())), "storage": "f32"}
+        ctx.close()
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -412,6 +458,9 @@ def main():
                "sample": f"{n} full {args.size}^3 evaluations of the FP64 oracle over "
                          f"{el:.1f} s (OpenMP, all host cores); the reference has no CPU LC2 path"}
 
+    small = None
+    if rank == 0 and not args.no_small:
+        small = small_configs(local)
     serve = None
     if rank == 0 and not args.no_serve:
         serve = serve_leg(args, case, local)
@@ -433,6 +482,7 @@ def main():
                     "d2h_bytes_per_step": K * 8},
             "plain": {"value": plain_eps, "unit": UNIT, "evals": P,
                       "batched_over_plain": value / world / plain_eps},
+            "small_configs": small,
             "serve": serve,
             "gpu_launches": launches,
             "clocks": clk.summary(),
