@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="default launch options")
     ap.add_argument("--no-small", action="store_true", help="skip the 2D 256^2 / 3D 96^3 lines")
+    ap.add_argument("--no-stack", action="store_true", help="skip the 2D-to-3D frame-stack line")
+    ap.add_argument("--stack-frames", type=int, default=64)
+    ap.add_argument("--stack-poses", type=int, default=256)
     ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--serve-rate", type=float, default=4.0, help="Poisson arrivals per second")
     ap.add_argument("--serve-active", type=int, default=8)
@@ -306,6 +309,45 @@ def small_configs(device):
     return out
 
 
+def stack_leg(args, main_case, device):
+    """2D-to-3D frame stack: frames of uneven sizes (sides 128-512 at 0.5 mm)
+    cut from the 256^3 MR at seeded 6-DOF poses, `stack_poses` candidate
+    poses per frame, all (frame, pose) pairs in one lc2_stack_evaluate call
+    (one persistent launch, replayed from a CUDA graph after the first)."""
+    import numpy as np
+
+    from lc2registration_gb300 import capi, synth
+    from tests.helpers import perturbed
+
+    frames = synth.frame_stack(main_case.moving, main_case.moving_geom, args.stack_frames,
+                               seed=91, spacing=0.5, r=3)
+    st = capi.Stack(main_case.moving_geom, 3, "f16", device)
+    st.set_moving(main_case.moving)
+    rng = np.random.default_rng(92)
+    ids, mats = [], []
+    for i, f in enumerate(frames):
+        st.add_frame(f.fixed_geom, f.virt_spacing, f.fixed)
+        ids += [i] * args.stack_poses
+        mats.append(perturbed(f, rng, args.stack_poses, scale=0.5))
+    ids = np.array(ids, dtype=np.int32)
+    mats = np.concatenate(mats)
+    st.evaluate(ids, mats)  # capture
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        vals = st.evaluate(ids, mats)
+    el = (time.perf_counter() - t0) / reps
+    assert np.all(np.isfinite(vals)) and vals.max() > 0
+    px = sum(int(f.fixed_geom.dim[0]) * int(f.fixed_geom.dim[1]) for f in frames)
+    st.close()
+    return {"frames": len(frames), "poses_per_frame": args.stack_poses,
+            "evaluations_per_call": int(len(ids)), "frame_pixels": px,
+            "evals_per_s": len(ids) / el, "ms_per_call": el * 1e3,
+            "pixel_evals_per_s": px * args.stack_poses / el,
+            "note": "end to end through lc2_stack_evaluate (host poses in, host LC2 out), "
+                    "f16 storage, 7x7 patches, one graph-replayed launch per call"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -461,6 +503,9 @@ def main():
     small = None
     if rank == 0 and not args.no_small:
         small = small_configs(local)
+    stack = None
+    if rank == 0 and not args.no_stack:
+        stack = stack_leg(args, case, local)
     serve = None
     if rank == 0 and not args.no_serve:
         serve = serve_leg(args, case, local)
@@ -483,6 +528,7 @@ def main():
             "plain": {"value": plain_eps, "unit": UNIT, "evals": P,
                       "batched_over_plain": value / world / plain_eps},
             "small_configs": small,
+            "stack": stack,
             "serve": serve,
             "gpu_launches": launches,
             "clocks": clk.summary(),
