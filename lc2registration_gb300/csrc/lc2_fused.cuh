@@ -319,7 +319,27 @@ struct TileShared {
   int ib[3];       // its integer part
   float fb[3];     // and fraction
   float A[9];      // moving-pixel step per region pixel
+  int inside;      // every sample of the region lies strictly inside the moving image
 };
+
+// Bilinear counterpart of fused_sample_inside (2D moving image).
+template <typename TM>
+__device__ __forceinline__ float fused_sample_inside2(const TM* __restrict__ mov,
+                                                      const FusedParams& P, const float* A,
+                                                      const int* sb, const float* sf, int px,
+                                                      int py) {
+  const float dx = (float)px, dy = (float)py;
+  const float qx = fmaf(A[1], dy, fmaf(A[0], dx, sf[0]));
+  const float qy = fmaf(A[4], dy, fmaf(A[3], dx, sf[1]));
+  const float flx = floorf(qx), fly = floorf(qy);
+  const float rx = qx - flx, ry = qy - fly;
+  const unsigned mx = (unsigned)P.mx;
+  const unsigned b = (unsigned)(sb[0] + (int)flx) + (unsigned)(sb[1] + (int)fly) * mx;
+  float f0 = ldf(mov, b), f1 = ldf(mov, b + mx);
+  float c0 = ldf(mov, b + 1), c1 = ldf(mov, b + 1 + mx);
+  float xl = fmaf(ry, f1 - f0, f0), xr = fmaf(ry, c1 - c0, c0);
+  return fmaf(rx, xr - xl, xl);
+}
 
 // One 32 x TY output tile of a 2D window (2D, or a 2D-to-3D frame when
 // WND = 3): resample the halo region, Sobel, limbs, x/y window passes and the
@@ -354,15 +374,38 @@ __device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
     }
 #pragma unroll
     for (int i = 0; i < 9; ++i) T.A[i] = (float)X->A[i];
+    // region in the virtual grid and every sample strictly inside the moving
+    // image (corners bound the affine image; 0.01 voxel covers float rounding)
+    bool in = gx0 >= 0 && gx0 + G::PW <= P.vx && gy0 >= 0 && gy0 + G::PH <= P.vy;
+    const int dims[3] = {P.mx, P.my, P.mz};
+#pragma unroll
+    for (int a = 0; a < WND; ++a) {
+      const float ex = T.A[3 * a] * (float)(G::PW - 1), ey = T.A[3 * a + 1] * (float)(G::PH - 1);
+      const float lo = T.fb[a] + fminf(ex, 0.0f) + fminf(ey, 0.0f);
+      const float hi = T.fb[a] + fmaxf(ex, 0.0f) + fmaxf(ey, 0.0f);
+      in = in && ((float)T.ib[a] + lo >= 0.01f) &&
+           ((float)T.ib[a] + hi <= (float)(dims[a] - 1) - 0.01f);
+    }
+    T.inside = in ? 1 : 0;
   }
   __syncthreads();
-  for (int i = tid; i < G::NPW; i += NT) {
-    const int py = i / G::PW, px = i - py * G::PW;
-    const int gx = gx0 + px, gy = gy0 + py;
-    float v = 0.0f;
-    if (gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy)
-      v = fused_sample<WND, TM>(mov, P, T.A, T.ib, T.fb, px, py);
-    mc[i] = v;
+  if (T.inside) {
+    for (int i = tid; i < G::NPW; i += NT) {
+      const int py = i / G::PW, px = i - py * G::PW;
+      if constexpr (WND == 3)
+        mc[i] = fused_sample_inside<TM>(mov, P, T.A, T.ib, T.fb, px, py);
+      else
+        mc[i] = fused_sample_inside2<TM>(mov, P, T.A, T.ib, T.fb, px, py);
+    }
+  } else {
+    for (int i = tid; i < G::NPW; i += NT) {
+      const int py = i / G::PW, px = i - py * G::PW;
+      const int gx = gx0 + px, gy = gy0 + py;
+      float v = 0.0f;
+      if (gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy)
+        v = fused_sample<WND, TM>(mov, P, T.A, T.ib, T.fb, px, py);
+      mc[i] = v;
+    }
   }
   __syncthreads();
   for (int p = tid; p < G::NP; p += NT) {
