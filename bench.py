@@ -222,6 +222,8 @@ def serve_leg(args, main_case, device):
         sent.append((k, tickets))
         time.sleep(rng.exponential(1.0 / args.serve_rate))
     lat = {k: [] for k in pools}
+    queue = {k: [] for k in pools}
+    run = {k: [] for k in pools}
     evals = 0
     for k, tickets in sent:
         rs = [srv.poll(t) for t in tickets]
@@ -229,6 +231,8 @@ def serve_leg(args, main_case, device):
             assert r["status"] == 0, r["message"]
             evals += r["evaluations"]
         lat[k].append(max(r["total_ms"] for r in rs))
+        queue[k].append(max(r["queue_ms"] for r in rs))
+        run[k].append(max(r["run_ms"] for r in rs))
     wall = time.perf_counter() - t0
     st = srv.stats()
     srv.close()
@@ -241,6 +245,8 @@ def serve_leg(args, main_case, device):
         "requests_per_s": len(sent) / wall, "evals_per_s": evals / wall,
         "p50_ms": pct(allv, 50), "p95_ms": pct(allv, 95), "p99_ms": pct(allv, 99),
         "by_kind_p50_ms": {k: pct(np.array(v), 50) for k, v in lat.items()},
+        "by_kind_mean_queue_ms": {k: float(np.mean(v)) if v else None for k, v in queue.items()},
+        "by_kind_mean_run_ms": {k: float(np.mean(v)) if v else None for k, v in run.items()},
         "by_kind_count": {k: len(v) for k, v in lat.items()},
         "max_active": args.serve_active, "peak_active": st["peak_active"],
         "peak_device_bytes": st["peak_bytes"],

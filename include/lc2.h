@@ -155,6 +155,11 @@ enum { LC2_OPTION_ZCHUNK = 2, LC2_OPTION_GRAPHS = 3 };
  * into a shared ring while consumer warps do the moments); 0 (default) the
  * single-role kernel. Same values either way. */
 enum { LC2_OPTION_PIPELINE = 4 };
+/* LC2_OPTION_STREAM_PRIORITY: recreates the context's own stream with this
+ * CUDA stream priority (lower = more urgent, clamped to the device's range;
+ * see cudaDeviceGetStreamPriorityRange). The server gives small requests the
+ * most urgent priority so their launches are scheduled ahead of large ones. */
+enum { LC2_OPTION_STREAM_PRIORITY = 5 };
 int lc2_set_option(lc2_context* ctx, int option, int value);
 
 /* CUDA-graph launches issued by lc2_evaluate_batch / lc2_evaluate. */

@@ -29,6 +29,7 @@ OPTION_TILE_ROWS = 1
 OPTION_ZCHUNK = 2
 OPTION_GRAPHS = 3
 OPTION_PIPELINE = 4
+OPTION_STREAM_PRIORITY = 5
 STORAGE = {"f32": 0, "f16": 1, "bf16": 2}
 
 # Every symbol include/lc2.h declares (checked by the test suite).

@@ -795,6 +795,23 @@ int lc2_set_option(lc2_context* c, int option, int value) {
     drop_graphs(c);
     return LC2_OK;
   }
+  if (option == LC2_OPTION_STREAM_PRIORITY) {
+    // recreate the context's own stream with this priority (clamped to the
+    // device's range); a caller-set stream is left alone
+    LC2_TRY(select_device(c));
+    int least = 0, greatest = 0;
+    LC2_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    const int prio = std::max(greatest, std::min(least, value));
+    cudaStream_t ns = nullptr;
+    LC2_CUDA(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, prio));
+    LC2_CUDA(cudaStreamSynchronize(c->own_stream));
+    drop_graphs(c);
+    const bool own = (c->stream == c->own_stream);
+    cudaStreamDestroy(c->own_stream);
+    c->own_stream = ns;
+    if (own) c->stream = ns;
+    return LC2_OK;
+  }
   if (option == LC2_OPTION_PIPELINE) {
     c->pipeline = value != 0;
     drop_graphs(c);

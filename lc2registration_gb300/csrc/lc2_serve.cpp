@@ -9,7 +9,8 @@
 // stream lets the kernels of concurrent requests overlap on the GPU. Memory
 // is returned and the next request admitted as each one completes
 // (continuous admission, not a fixed batch). Admission is strictly in arrival
-// order, so a large request is never starved by smaller ones behind it.
+// order, so a large request is never starved by smaller ones behind it; on
+// the GPU, small requests run on the most urgent stream priority.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -86,6 +87,13 @@ struct lc2_server {
       lc2_config cfg = j.req.config;
       cfg.device = this->cfg.device;
       st = lc2_create(&cfg, &c);
+      // small requests (virtual grid up to 2^20 voxels) on the most urgent
+      // stream priority: their short launches are scheduled ahead of the
+      // CTAs of large concurrent ones
+      int vd[3] = {0, 0, 0};
+      if (st == LC2_OK && lc2_virtual_dims(c, vd) == LC2_OK &&
+          (long long)vd[0] * vd[1] * vd[2] <= (1LL << 20))
+        st = lc2_set_option(c, LC2_OPTION_STREAM_PRIORITY, -1000);
       if (st == LC2_OK) st = lc2_set_images(c, j.fixed.data(), j.moving.data());
       if (st == LC2_OK) st = lc2_register(c, &reg, &out);
       std::string msg = st != LC2_OK ? lc2_last_error() : "";

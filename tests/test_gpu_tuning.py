@@ -87,3 +87,12 @@ def test_warp_specialised_kernel_equals_single_role(r):
         ctx.set_option(capi.OPTION_ZCHUNK, zc)
         np.testing.assert_array_equal(ctx.evaluate_batch(mats), ref)
         np.testing.assert_array_equal(_staged(ctx, mats), ref)
+
+
+def test_stream_priority_keeps_results(case3d):
+    ctx = make_context(case3d)
+    mats = perturbed(case3d, np.random.default_rng(6), 4)
+    ref = ctx.evaluate_batch(mats)
+    ctx.set_option(capi.OPTION_STREAM_PRIORITY, -1000)
+    np.testing.assert_array_equal(ctx.evaluate_batch(mats), ref)
+    np.testing.assert_array_equal(_staged(ctx, mats), ref)
