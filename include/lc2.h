@@ -374,6 +374,15 @@ int lc2_stack_evaluate(lc2_stack* s, int count, const int* frame_ids, const floa
                        double* lc2);
 /* CUDA-graph replay of repeated layouts: on (1, default) or off (0). */
 int lc2_stack_set_graphs(lc2_stack* s, int on);
+/* Registers n frames at once (Optimizers2DTo3D per frame,
+ * src/Optimizers/optimizers.cu:1195-1640): regs[i] (mode LC2_MODE_2DTO3D)
+ * on frame frame_ids[i], each on its own host thread, with every round of
+ * their optimizer steps evaluated as one stack launch. results[i] equals
+ * lc2_register on that frame's context alone. statuses (may be NULL): per
+ * registration lc2_status; *launches (may be NULL): stack evaluations issued.
+ * Returns the first failure, else LC2_OK. */
+int lc2_stack_register(lc2_stack* s, int n, const int* frame_ids, const lc2_registration* regs,
+                       lc2_registration_result* results, int* statuses, long long* launches);
 /* Kernel launches and graph launches issued by the stack since creation. */
 long long lc2_stack_launch_count(const lc2_stack* s);
 long long lc2_stack_graph_launches(const lc2_stack* s);

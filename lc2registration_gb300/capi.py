@@ -46,7 +46,7 @@ EXPORTED = [
     "lc2_server_create", "lc2_server_submit", "lc2_server_poll", "lc2_server_drain",
     "lc2_server_get_stats", "lc2_server_reset_stats", "lc2_server_destroy",
     "lc2_graph_launches", "lc2_autotune", "lc2_get_config", "lc2_weighting_map",
-    "lc2_warp_affine_2d",
+    "lc2_warp_affine_2d", "lc2_stack_register",
 ]
 
 ALGORITHMS = {"direct_l": 1, "bobyqa": 2, "nelder_mead": 3}
@@ -192,6 +192,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "lc2_stack_set_graphs": ([vp, ctypes.c_int], ctypes.c_int),
         "lc2_stack_launch_count": ([vp], ctypes.c_longlong),
         "lc2_stack_graph_launches": ([vp], ctypes.c_longlong),
+        "lc2_stack_register": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                ctypes.POINTER(lc2_registration),
+                                ctypes.POINTER(lc2_registration_result),
+                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong)],
+                               ctypes.c_int),
         "lc2_context_bytes": ([ctypes.POINTER(lc2_config), ctypes.POINTER(ctypes.c_size_t),
                                ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
         "lc2_server_create": ([ctypes.POINTER(lc2_server_config), ctypes.POINTER(vp)],
@@ -466,6 +471,25 @@ class Stack:
 
     def set_graphs(self, on: bool):
         _check(self._lib.lc2_stack_set_graphs(self._h, int(bool(on))))
+
+    def register(self, frame_ids, registrations):
+        """lc2_stack_register: registrations = list of make_registration
+        keyword dicts (mode is 2DTo3D), one per frame id. Returns (list of
+        result dicts, stack launches)."""
+        n = len(frame_ids)
+        ids = (ctypes.c_int * n)(*[int(i) for i in frame_ids])
+        regs = (lc2_registration * n)()
+        keep = []
+        for i, kw in enumerate(registrations):
+            regs[i] = make_registration("2DTo3D", keep=keep, **kw)
+        res = (lc2_registration_result * n)()
+        sts = (ctypes.c_int * n)()
+        launches = ctypes.c_longlong()
+        _check(self._lib.lc2_stack_register(self._h, n, ids, regs, res, sts,
+                                            ctypes.byref(launches)))
+        out = [dict(params=np.array(r.params[:12]), lc2=r.lc2, evaluations=r.evaluations,
+                    launches=r.launches) for r in res]
+        return out, launches.value
 
     def launch_count(self) -> int:
         return int(self._lib.lc2_stack_launch_count(self._h))

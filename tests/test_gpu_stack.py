@@ -120,3 +120,25 @@ def test_stack_errors():
     with pytest.raises(capi.LC2Error, match="share"):
         fc.set_images(f.fixed, mr)
     assert st.evaluate([], np.zeros((0, 16))).shape == (0,)
+
+
+def test_stack_register_equals_per_frame_registration():
+    mr, mg, frames = _frames(4, seed=45, sides=(40, 56, 72))
+    st = _stack(mr, mg, frames, 3)
+    lo = [-6, -6, -6, -6, -6, -6, 0.95, 0.95, 0.95, -0.02, -0.02, -0.02]
+    hi = [6, 6, 6, 6, 6, 6, 1.05, 1.05, 1.05, 0.02, 0.02, 0.02]
+    regs = []
+    for f in frames:
+        regs.append(dict(initial=[0, 0, 0, 0, 0, 0, 1, 1, 1, 0, 0, 0], lower=lo, upper=hi,
+                         center=f.fixed_geom.center(), direct_entries=["translation"],
+                         direct_maxeval=30, rounds=[(["translation", "rotation"], 1e-3)]))
+    got, launches = st.register(list(range(len(frames))), regs)
+    total_batches = 0
+    for i, f in enumerate(frames):
+        alone = capi.register(make_context(f), **regs[i])
+        np.testing.assert_array_equal(got[i]["params"], alone["params"])
+        assert got[i]["lc2"] == alone["lc2"]
+        assert got[i]["evaluations"] == alone["evaluations"]
+        total_batches += alone["launches"]
+    # every round of optimizer steps of all frames went out as one stack call
+    assert launches < total_batches
