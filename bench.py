@@ -216,9 +216,11 @@ def serve_leg(args, main_case, device):
         pool = pools[k]
         item = pool[int(rng.integers(len(pool)))]
         if k == "stack16":
-            tickets = [submit(f, "f32") for f in item]
+            tickets = [("stack", srv.submit_stack(
+                main_case.moving_geom, main_case.moving, 3, [(f.fixed_geom, f.fixed) for f in item],
+                item[0].virt_spacing, [_registration(f, rng) for f in item], "f16"))]
         else:
-            tickets = [submit(item, "f16" if k == "3d_256_f16" else "f32")]
+            tickets = [("one", submit(item, "f16" if k == "3d_256_f16" else "f32"))]
         sent.append((k, tickets))
         time.sleep(rng.exponential(1.0 / args.serve_rate))
     lat = {k: [] for k in pools}
@@ -226,7 +228,9 @@ def serve_leg(args, main_case, device):
     run = {k: [] for k in pools}
     evals = 0
     for k, tickets in sent:
-        rs = [srv.poll(t) for t in tickets]
+        rs = []
+        for kind, t in tickets:
+            rs += srv.poll_stack(t) if kind == "stack" else [srv.poll(t)]
         for r in rs:
             assert r["status"] == 0, r["message"]
             evals += r["evaluations"]
@@ -251,7 +255,8 @@ def serve_leg(args, main_case, device):
         "max_active": args.serve_active, "peak_active": st["peak_active"],
         "peak_device_bytes": st["peak_bytes"],
         "mix": "40% 2D 256^2 r3, 30% 3D 128^3->96^3 r3, 20% 3D 256^3 f16 r4, 10% 2D-to-3D "
-               "stacks of 16 frames (sides 128-512 at 0.5 mm) r3; DIRECT + 2 rounds to xtol 1e-6",
+               "stacks of 16 frames (sides 128-512 at 0.5 mm, one stack request sharing one "
+               "upload of the volume) r3; DIRECT + 2 rounds to xtol 1e-6",
     }
 
 

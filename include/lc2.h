@@ -320,6 +320,22 @@ typedef struct {
     double elapsed_s;                /* since creation or the last reset */
 } lc2_server_stats;
 
+/* A 2D-to-3D stack request: one moving volume, `frames` ultrasound frames
+ * (geometries frame_geoms[i], images frame_images[i], one shared virtual
+ * spacing) and one registration per frame (mode LC2_MODE_2DTO3D), run as
+ * lc2_stack_register. Host buffers are copied by the submit call. */
+typedef struct {
+    lc2_geometry moving;
+    const float* moving_image;
+    int patch_size;
+    int storage;
+    int frames;
+    const lc2_geometry* frame_geoms;
+    const float* const* frame_images;
+    float virtual_spacing[3];
+    const lc2_registration* registrations;
+} lc2_stack_request;
+
 /* Device bytes a context of this configuration holds (*held) and at most
  * while lc2_set_images runs (*peak, may be NULL). No device work. */
 int lc2_context_bytes(const lc2_config* cfg, size_t* held, size_t* peak);
@@ -327,6 +343,12 @@ int lc2_server_create(const lc2_server_config* cfg, lc2_server** out);
 /* Queues a request; *ticket identifies it. LC2_ERR_OUT_OF_MEMORY when the
  * request alone exceeds the budget. */
 int lc2_server_submit(lc2_server* s, const lc2_request* req, long long* ticket);
+/* Queues a stack request; polled with lc2_server_poll_stack. */
+int lc2_server_submit_stack(lc2_server* s, const lc2_stack_request* req, long long* ticket);
+/* As lc2_server_poll for a stack request: out receives one result per frame
+ * (`frames` entries), each with the request's queue / run / total times. */
+int lc2_server_poll_stack(lc2_server* s, long long ticket, int wait_ms, lc2_request_result* out,
+                          int frames);
 /* Waits up to wait_ms (-1 = no limit) for the request; LC2_ERR_NOT_READY
  * while it is queued or running. A completed result is returned once. */
 int lc2_server_poll(lc2_server* s, long long ticket, int wait_ms, lc2_request_result* out);
@@ -374,6 +396,15 @@ int lc2_stack_evaluate(lc2_stack* s, int count, const int* frame_ids, const floa
                        double* lc2);
 /* CUDA-graph replay of repeated layouts: on (1, default) or off (0). */
 int lc2_stack_set_graphs(lc2_stack* s, int on);
+/* LC2_OPTION_GRAPHS and LC2_OPTION_STREAM_PRIORITY for the stack's own
+ * stream (as lc2_set_option), and LC2_OPTION_STACK_BATCHING for
+ * lc2_stack_register: 1 (default) evaluates every round of the frames'
+ * optimizer steps as one stack launch (throughput), 0 runs the frames'
+ * registrations independently and concurrently on their own contexts and
+ * streams (latency; frame ids must then be distinct). Same results. */
+enum { LC2_OPTION_STACK_BATCHING = 6 };
+int lc2_stack_set_option(lc2_stack* s, int option, int value);
+int lc2_stack_get_option(const lc2_stack* s, int option, int* value);
 /* Registers n frames at once (Optimizers2DTo3D per frame,
  * src/Optimizers/optimizers.cu:1195-1640): regs[i] (mode LC2_MODE_2DTO3D)
  * on frame frame_ids[i], each on its own host thread, with every round of

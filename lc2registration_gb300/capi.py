@@ -30,6 +30,7 @@ OPTION_ZCHUNK = 2
 OPTION_GRAPHS = 3
 OPTION_PIPELINE = 4
 OPTION_STREAM_PRIORITY = 5
+OPTION_STACK_BATCHING = 6
 STORAGE = {"f32": 0, "f16": 1, "bf16": 2}
 
 # Every symbol include/lc2.h declares (checked by the test suite).
@@ -46,7 +47,8 @@ EXPORTED = [
     "lc2_server_create", "lc2_server_submit", "lc2_server_poll", "lc2_server_drain",
     "lc2_server_get_stats", "lc2_server_reset_stats", "lc2_server_destroy",
     "lc2_graph_launches", "lc2_autotune", "lc2_get_config", "lc2_weighting_map",
-    "lc2_warp_affine_2d", "lc2_stack_register",
+    "lc2_warp_affine_2d", "lc2_stack_register", "lc2_server_submit_stack",
+    "lc2_server_poll_stack", "lc2_stack_set_option", "lc2_stack_get_option",
 ]
 
 ALGORITHMS = {"direct_l": 1, "bobyqa": 2, "nelder_mead": 3}
@@ -120,6 +122,15 @@ class lc2_request_result(ctypes.Structure):
                 ("result", lc2_registration_result), ("queue_ms", ctypes.c_double),
                 ("run_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
                 ("device_bytes", ctypes.c_size_t), ("admission", ctypes.c_longlong)]
+
+
+class lc2_stack_request(ctypes.Structure):
+    _fields_ = [("moving", lc2_geometry), ("moving_image", ctypes.POINTER(ctypes.c_float)),
+                ("patch_size", ctypes.c_int), ("storage", ctypes.c_int), ("frames", ctypes.c_int),
+                ("frame_geoms", ctypes.POINTER(lc2_geometry)),
+                ("frame_images", ctypes.POINTER(ctypes.POINTER(ctypes.c_float))),
+                ("virtual_spacing", ctypes.c_float * 3),
+                ("registrations", ctypes.POINTER(lc2_registration))]
 
 
 class lc2_server_stats(ctypes.Structure):
@@ -209,6 +220,13 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "lc2_server_get_stats": ([vp, ctypes.POINTER(lc2_server_stats)], ctypes.c_int),
         "lc2_server_reset_stats": ([vp], ctypes.c_int),
         "lc2_server_destroy": ([vp], ctypes.c_int),
+        "lc2_server_submit_stack": ([vp, ctypes.POINTER(lc2_stack_request),
+                                     ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+        "lc2_server_poll_stack": ([vp, ctypes.c_longlong, ctypes.c_int,
+                                   ctypes.POINTER(lc2_request_result), ctypes.c_int],
+                                  ctypes.c_int),
+        "lc2_stack_set_option": ([vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "lc2_stack_get_option": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "lc2_graph_launches": ([vp], ctypes.c_longlong),
         "lc2_get_config": ([vp, ctypes.POINTER(lc2_config)], ctypes.c_int),
         "lc2_weighting_map": ([vp, _fp, _dp, _fp], ctypes.c_int),
@@ -472,6 +490,9 @@ class Stack:
     def set_graphs(self, on: bool):
         _check(self._lib.lc2_stack_set_graphs(self._h, int(bool(on))))
 
+    def set_option(self, option: int, value: int):
+        _check(self._lib.lc2_stack_set_option(self._h, int(option), int(value)))
+
     def register(self, frame_ids, registrations):
         """lc2_stack_register: registrations = list of make_registration
         keyword dicts (mode is 2DTo3D), one per frame id. Returns (list of
@@ -701,6 +722,7 @@ class Server:
         _check(lib.lc2_server_create(ctypes.byref(cfg), ctypes.byref(self._h)))
         self._keep = {}   # ticket -> callback objects the C side may still call
         self._errs = {}
+        self._stack_n = {}  # ticket -> frames of a stack request
 
     def close(self):
         if self._h:
@@ -752,6 +774,50 @@ class Server:
                     lc2=r.lc2, evaluations=r.evaluations, launches=r.launches,
                     queue_ms=out.queue_ms, run_ms=out.run_ms, total_ms=out.total_ms,
                     device_bytes=out.device_bytes, admission=out.admission)
+
+    def submit_stack(self, moving_geom: Geometry, moving, patch_size: int, frames,
+                     virt_spacing, registrations, storage: str = "f32") -> int:
+        """One 2D-to-3D stack request: frames = [(Geometry, image)], one
+        make_registration keyword dict per frame."""
+        n = len(frames)
+        req = lc2_stack_request()
+        req.moving = _geom(moving_geom)
+        mv = _f32(moving)
+        req.moving_image = mv.ctypes.data_as(_fp)
+        req.patch_size = int(patch_size)
+        req.storage = STORAGE[storage]
+        req.frames = n
+        geoms = (lc2_geometry * n)(*[_geom(g) for g, _ in frames])
+        imgs = [_f32(im) for _, im in frames]
+        ptrs = (ctypes.POINTER(ctypes.c_float) * n)(*[im.ctypes.data_as(_fp) for im in imgs])
+        req.frame_geoms = geoms
+        req.frame_images = ptrs
+        vs = list(virt_spacing) + [1.0] * (3 - len(virt_spacing))
+        for a in range(3):
+            req.virtual_spacing[a] = float(vs[a])
+        regs = (lc2_registration * n)()
+        keep = []
+        for i, kw in enumerate(registrations):
+            regs[i] = make_registration("2DTo3D", keep=keep, **kw)
+        req.registrations = regs
+        t = ctypes.c_longlong()
+        _check(self._lib.lc2_server_submit_stack(self._h, ctypes.byref(req), ctypes.byref(t)))
+        self._keep[t.value] = keep
+        self._stack_n[t.value] = n
+        return t.value
+
+    def poll_stack(self, ticket: int, wait_ms: int = -1):
+        """Per-frame result dicts, or None while the request is queued or running."""
+        n = self._stack_n.get(ticket, 1)
+        out = (lc2_request_result * n)()
+        st = self._lib.lc2_server_poll_stack(self._h, int(ticket), int(wait_ms), out, n)
+        if st == 4:
+            return None
+        _check(st)
+        self._keep.pop(ticket, None)
+        return [dict(status=o.status, message=o.message.decode(), params=np.array(o.result.params[:]),
+                     lc2=o.result.lc2, evaluations=o.result.evaluations, queue_ms=o.queue_ms,
+                     run_ms=o.run_ms, total_ms=o.total_ms, admission=o.admission) for o in out]
 
     def drain(self, wait_ms: int = -1) -> bool:
         st = self._lib.lc2_server_drain(self._h, int(wait_ms))

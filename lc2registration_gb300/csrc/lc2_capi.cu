@@ -1466,6 +1466,7 @@ struct lc2_stack {
   };
   std::vector<Graph> graphs;
   bool use_graphs = true;
+  bool batching = true;  // lc2_stack_register: lock-step merged launches
   long long launches = 0, graph_launches = 0;
 };
 
@@ -1677,6 +1678,42 @@ int lc2_stack_set_graphs(lc2_stack* s, int on) {
   if (!s) return fail(LC2_ERR_INVALID_ARGUMENT, "null stack");
   s->use_graphs = on != 0;
   return LC2_OK;
+}
+
+int lc2_stack_set_option(lc2_stack* s, int option, int value) {
+  if (!s) return fail(LC2_ERR_INVALID_ARGUMENT, "null stack");
+  if (option == LC2_OPTION_GRAPHS) return lc2_stack_set_graphs(s, value);
+  if (option == LC2_OPTION_STACK_BATCHING) {
+    s->batching = value != 0;
+    return LC2_OK;
+  }
+  if (option == LC2_OPTION_STREAM_PRIORITY) {
+    LC2_TRY(stack_select_device(s));
+    int least = 0, greatest = 0;
+    LC2_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    const int prio = std::max(greatest, std::min(least, value));
+    cudaStream_t ns = nullptr;
+    LC2_CUDA(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, prio));
+    LC2_CUDA(cudaStreamSynchronize(s->stream));
+    stack_drop_graphs(s);
+    cudaStreamDestroy(s->stream);
+    s->stream = ns;
+    return LC2_OK;
+  }
+  return fail(LC2_ERR_INVALID_ARGUMENT, "unknown stack option %d", option);
+}
+
+int lc2_stack_get_option(const lc2_stack* s, int option, int* value) {
+  if (!s || !value) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  if (option == LC2_OPTION_STACK_BATCHING) {
+    *value = s->batching ? 1 : 0;
+    return LC2_OK;
+  }
+  if (option == LC2_OPTION_GRAPHS) {
+    *value = s->use_graphs ? 1 : 0;
+    return LC2_OK;
+  }
+  return fail(LC2_ERR_INVALID_ARGUMENT, "unknown stack option %d", option);
 }
 
 long long lc2_stack_launch_count(const lc2_stack* s) { return s ? s->launches : 0; }

@@ -48,6 +48,13 @@ struct Job {
   long long ticket = 0;
   lc2_request req{};
   std::vector<float> fixed, moving;
+  // stack requests: frames registered together on one shared moving volume
+  bool is_stack = false;
+  lc2_stack_request sreq{};
+  std::vector<lc2_geometry> frame_geoms;
+  std::vector<std::vector<float>> frame_images;
+  std::vector<lc2_registration> frame_regs;
+  std::vector<lc2_request_result> frame_res;
   size_t bytes = 0;
   enum { Queued, Running, Done } state = Queued;
   lc2_request_result res{};
@@ -76,7 +83,49 @@ struct lc2_server {
   std::vector<double> latencies;  // total_ms of completed requests
   Clock::time_point t0 = Clock::now();
 
+  // A stack request: the frames register concurrently on their own contexts
+  // and streams (latency first), sharing one upload of the moving volume.
+  void run_stack(Job& j) {
+    const lc2_stack_request& q = j.sreq;
+    const int n = (int)j.frame_geoms.size();
+    j.frame_res.assign(n, lc2_request_result{});
+    lc2_stack* st = nullptr;
+    int status = lc2_stack_create(&q.moving, q.patch_size, q.storage, cfg.device, &st);
+    // frames are small 2D grids: the most urgent stream priority, as small requests
+    if (status == LC2_OK) status = lc2_stack_set_option(st, LC2_OPTION_STREAM_PRIORITY, -1000);
+    if (status == LC2_OK) status = lc2_stack_set_option(st, LC2_OPTION_STACK_BATCHING, 0);
+    if (status == LC2_OK) status = lc2_stack_set_moving(st, j.moving.data());
+    std::vector<int> ids(n);
+    for (int i = 0; i < n && status == LC2_OK; ++i)
+      status = lc2_stack_add_frame(st, &j.frame_geoms[i], q.virtual_spacing,
+                                   j.frame_images[i].data(), &ids[i]);
+    for (int i = 0; i < n && status == LC2_OK; ++i) {
+      lc2_context* fc = nullptr;
+      status = lc2_stack_frame_context(st, ids[i], &fc);
+      if (status == LC2_OK) status = lc2_set_option(fc, LC2_OPTION_STREAM_PRIORITY, -1000);
+    }
+    std::vector<lc2_registration_result> rr(n);
+    std::vector<int> sts(n, status);
+    if (status == LC2_OK)
+      status = lc2_stack_register(st, n, ids.data(), j.frame_regs.data(), rr.data(), sts.data(),
+                                  nullptr);
+    const std::string msg = status != LC2_OK ? lc2_last_error() : "";
+    if (st) lc2_stack_destroy(st);
+    for (int i = 0; i < n; ++i) {
+      j.frame_res[i].status = sts[i];
+      j.frame_res[i].result = rr[i];
+      if (sts[i] != LC2_OK)
+        std::snprintf(j.frame_res[i].message, sizeof(j.frame_res[i].message), "%s", msg.c_str());
+    }
+    j.res.status = status;
+    if (status != LC2_OK) std::snprintf(j.res.message, sizeof(j.res.message), "%s", msg.c_str());
+  }
+
   void run(Job& j) {
+    if (j.is_stack) {
+      run_stack(j);
+      return;
+    }
     lc2_registration reg = j.req.registration;
     lc2_registration_result out{};
     int st;
@@ -138,6 +187,14 @@ struct lc2_server {
         j->fixed.shrink_to_fit();
         j->moving.clear();
         j->moving.shrink_to_fit();
+        j->frame_images.clear();
+        for (auto& r : j->frame_res) {
+          r.queue_ms = j->res.queue_ms;
+          r.run_ms = j->res.run_ms;
+          r.total_ms = j->res.total_ms;
+          r.device_bytes = j->bytes;
+          r.admission = j->res.admission;
+        }
         used -= j->bytes;
         --active;
         if (j->res.status == LC2_OK) {
@@ -213,12 +270,94 @@ int lc2_server_submit(lc2_server* s, const lc2_request* req, long long* ticket) 
   return LC2_OK;
 }
 
+static int enqueue_job(lc2_server* s, std::shared_ptr<Job> j, long long* ticket) {
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stop) return fail(LC2_ERR_NOT_READY, "server is shutting down");
+    j->ticket = s->next_ticket++;
+    j->t_submit = Clock::now();
+    s->queue.push_back(j);
+    s->jobs[j->ticket] = j;
+    ++s->submitted;
+    *ticket = j->ticket;
+  }
+  s->cv_admit.notify_all();
+  return LC2_OK;
+}
+
+int lc2_server_submit_stack(lc2_server* s, const lc2_stack_request* req, long long* ticket) {
+  if (!s || !req || !ticket || !req->moving_image || req->frames < 1 || !req->frame_geoms ||
+      !req->frame_images || !req->registrations)
+    return fail(LC2_ERR_INVALID_ARGUMENT, "incomplete stack request");
+  // device footprint: the moving volume once, each frame's own buffers
+  size_t bytes = 0, held = 0, peak = 0;
+  lc2_config fc{};
+  fc.mode = LC2_MODE_2DTO3D;
+  fc.moving = req->moving;
+  fc.patch_size = req->patch_size;
+  fc.high_res_is_moving = 1;
+  fc.storage = req->storage;
+  fc.max_batch = 1;
+  for (int a = 0; a < 3; ++a) fc.virtual_spacing[a] = req->virtual_spacing[a];
+  const size_t nm = (size_t)req->moving.dim[0] * req->moving.dim[1] * req->moving.dim[2];
+  const size_t es = req->storage == LC2_STORE_F32 ? 4 : 2;
+  for (int i = 0; i < req->frames; ++i) {
+    fc.fixed = req->frame_geoms[i];
+    int st = lc2_context_bytes(&fc, &held, &peak);
+    if (st != LC2_OK) return st;
+    bytes += held - nm * es;  // the frames share the stack's moving volume
+  }
+  bytes += nm * (es + sizeof(float));  // the volume and its upload staging
+  if (bytes > s->cfg.hbm_budget_bytes)
+    return fail(LC2_ERR_OUT_OF_MEMORY, "stack request needs " + std::to_string(bytes) +
+                                           " device bytes, the budget is " +
+                                           std::to_string(s->cfg.hbm_budget_bytes));
+  auto j = std::make_shared<Job>();
+  j->is_stack = true;
+  j->sreq = *req;
+  j->bytes = bytes;
+  j->moving.assign(req->moving_image, req->moving_image + nm);
+  for (int i = 0; i < req->frames; ++i) {
+    const lc2_geometry& g = req->frame_geoms[i];
+    j->frame_geoms.push_back(g);
+    j->frame_images.emplace_back(req->frame_images[i],
+                                 req->frame_images[i] + (size_t)g.dim[0] * g.dim[1] * g.dim[2]);
+    j->frame_regs.push_back(req->registrations[i]);
+  }
+  j->sreq.moving_image = nullptr;
+  j->sreq.frame_geoms = nullptr;
+  j->sreq.frame_images = nullptr;
+  j->sreq.registrations = nullptr;
+  return enqueue_job(s, j, ticket);
+}
+
+int lc2_server_poll_stack(lc2_server* s, long long ticket, int wait_ms, lc2_request_result* out,
+                          int frames) {
+  if (!s || !out) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(ticket);
+  if (it == s->jobs.end()) return fail(LC2_ERR_INVALID_ARGUMENT, "unknown or already returned ticket");
+  std::shared_ptr<Job> j = it->second;
+  if (!j->is_stack || (int)j->frame_geoms.size() != frames)
+    return fail(LC2_ERR_INVALID_ARGUMENT, "not a stack request of that many frames");
+  auto done = [&] { return j->state == Job::Done; };
+  if (wait_ms < 0)
+    s->cv_done.wait(lk, done);
+  else
+    s->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), done);
+  if (!done()) return fail(LC2_ERR_NOT_READY, "request still queued or running");
+  for (int i = 0; i < frames; ++i) out[i] = j->frame_res[i];
+  s->jobs.erase(ticket);
+  return LC2_OK;
+}
+
 int lc2_server_poll(lc2_server* s, long long ticket, int wait_ms, lc2_request_result* out) {
   if (!s || !out) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
   std::unique_lock<std::mutex> lk(s->mu);
   auto it = s->jobs.find(ticket);
   if (it == s->jobs.end()) return fail(LC2_ERR_INVALID_ARGUMENT, "unknown or already returned ticket");
   std::shared_ptr<Job> j = it->second;
+  if (j->is_stack) return fail(LC2_ERR_INVALID_ARGUMENT, "a stack request: use lc2_server_poll_stack");
   auto done = [&] { return j->state == Job::Done; };
   if (wait_ms < 0)
     s->cv_done.wait(lk, done);

@@ -9,10 +9,12 @@
 // frame still registering has submitted its step, the last one to arrive
 // launches all of them as one lc2_stack_evaluate call (one work-list launch,
 // graph-replayed when the layout repeats) and hands the values back. A frame
-// that finishes leaves the batcher, so the others never wait for it. Stack
-// values equal the frame's standalone values bit for bit and the optimizers
-// are deterministic, so each frame's result equals lc2_register run on that
-// frame alone.
+// that finishes leaves the batcher, so the others never wait for it. With
+// LC2_OPTION_STACK_BATCHING off, each thread instead registers its frame on
+// the frame's own context and stream, independently of the others (lower
+// latency when the GPU is shared). Stack values equal the frame's standalone
+// values bit for bit and the optimizers are deterministic, so each frame's
+// result equals lc2_register run on that frame alone either way.
 #include <condition_variable>
 #include <cstdio>
 #include <mutex>
@@ -142,6 +144,20 @@ extern "C" int lc2_stack_register(lc2_stack* s, int n, const int* frame_ids,
       return LC2_ERR_INVALID_ARGUMENT;
     }
   }
+  int batching = 1;
+  lc2_stack_get_option(s, LC2_OPTION_STACK_BATCHING, &batching);
+  std::vector<lc2_context*> ctx(n, nullptr);
+  if (!batching) {
+    std::vector<char> seen(nf, 0);
+    for (int i = 0; i < n; ++i) {
+      if (seen[frame_ids[i]]) {
+        lc2_set_error_message("lc2_stack_register: frame ids must be distinct without batching");
+        return LC2_ERR_INVALID_ARGUMENT;
+      }
+      seen[frame_ids[i]] = 1;
+      lc2_stack_frame_context(s, frame_ids[i], &ctx[i]);
+    }
+  }
   Batcher b(s, n);
   std::vector<Client> clients(n);
   std::vector<int> st(n, LC2_OK);
@@ -152,9 +168,13 @@ extern "C" int lc2_stack_register(lc2_stack* s, int n, const int* frame_ids,
     clients[i] = {&b, frame_ids[i]};
     threads.emplace_back([&, i] {
       lc2_registration r = regs[i];
-      r.lc2_of_matrices = &objective;
-      r.user = &clients[i];
-      st[i] = lc2_register(nullptr, &r, &results[i]);
+      if (batching) {
+        r.lc2_of_matrices = &objective;
+        r.user = &clients[i];
+        st[i] = lc2_register(nullptr, &r, &results[i]);
+      } else {
+        st[i] = lc2_register(ctx[i], &r, &results[i]);
+      }
       if (st[i] != LC2_OK) msgs[i] = lc2_last_error();
       b.leave();
     });

@@ -60,3 +60,30 @@ def test_mixed_stream_equals_alone():
     assert st["peak_active"] >= 2            # requests did overlap
     assert st["p99_ms"] >= st["p50_ms"] > 0
     srv.close()
+
+
+def test_stack_request_equals_stack_registration():
+    mr = synth.mr_phantom((48, 48, 48), 8, 1.5, seed=18)
+    mg = Geometry((48, 48, 48), (1.0, 1.0, 1.0), (0.0, 0.0, 0.0))
+    frames = synth.frame_stack(mr, mg, 3, seed=19, sides=(40, 56), spacing=0.5, r=3)
+    regs = [_reg(f) for f in frames]
+    st = capi.Stack(mg, 3)
+    st.set_moving(mr)
+    for f in frames:
+        st.add_frame(f.fixed_geom, f.virt_spacing, f.fixed)
+    want, _ = st.register(list(range(3)), regs)
+    srv = capi.Server(budget_bytes=2 << 30, max_active=2)
+    c2 = synth.case_2d(seed=20, size=64, r=3)
+    cfg = capi.make_config(c2.mode, c2.fixed_geom, c2.moving_geom, c2.virt_spacing, c2.r)
+    t_other = srv.submit(cfg, c2.fixed, c2.moving, **_reg(c2))
+    t = srv.submit_stack(mg, mr, 3, [(f.fixed_geom, f.fixed) for f in frames],
+                         frames[0].virt_spacing, regs)
+    got = srv.poll_stack(t)
+    assert srv.poll(t_other)["status"] == 0
+    for g, w in zip(got, want):
+        assert g["status"] == 0, g["message"]
+        np.testing.assert_array_equal(g["params"][:12], w["params"])
+        assert g["lc2"] == w["lc2"]
+    with pytest.raises(capi.LC2Error, match="unknown"):
+        srv.poll_stack(t)
+    srv.close()

@@ -142,3 +142,12 @@ def test_stack_register_equals_per_frame_registration():
         total_batches += alone["launches"]
     # every round of optimizer steps of all frames went out as one stack call
     assert launches < total_batches
+    # independent concurrent registrations on the frames' own contexts: same results
+    st.set_option(capi.OPTION_STACK_BATCHING, 0)
+    got2, launches2 = st.register(list(range(len(frames))), regs)
+    assert launches2 == 0
+    for a, b in zip(got, got2):
+        np.testing.assert_array_equal(a["params"], b["params"])
+        assert a["lc2"] == b["lc2"]
+    with pytest.raises(capi.LC2Error, match="distinct"):
+        st.register([0, 0], regs[:2])

@@ -121,3 +121,12 @@ def test_poll_timeout_and_drain():
     assert r1["admission"] == 0 and r2["admission"] == 1
     assert r2["queue_ms"] >= r1["run_ms"] * 0.5
     srv.close()
+
+
+def test_stack_request_validation():
+    import ctypes
+    srv = capi.Server(budget_bytes=1 << 40, max_active=1)
+    req = capi.lc2_stack_request()
+    t = ctypes.c_longlong()
+    assert srv._lib.lc2_server_submit_stack(srv._h, ctypes.byref(req), ctypes.byref(t)) == 1
+    srv.close()
