@@ -8,6 +8,8 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -49,6 +51,69 @@ int fail(int code, const char* fmt, ...) {
   } while (0)
 
 size_t elem_size(int storage) { return storage == LC2_STORE_F32 ? 4 : 2; }
+
+// Device memory comes from the device's default stream-ordered pool, set to
+// keep what is freed (release threshold: unlimited), so creating and
+// destroying contexts never synchronises the device: cudaFree would wait for
+// every stream, i.e. for other requests' kernels.
+cudaError_t dev_alloc(void** p, size_t n, cudaStream_t st) {
+  static std::mutex mu;
+  static std::vector<int> ready;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (std::find(ready.begin(), ready.end(), dev) == ready.end()) {
+      cudaMemPool_t pool;
+      e = cudaDeviceGetDefaultMemPool(&pool, dev);
+      if (e != cudaSuccess) return e;
+      unsigned long long keep = ~0ull;
+      e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+      if (e != cudaSuccess) return e;
+      ready.push_back(dev);
+    }
+  }
+  *p = nullptr;
+  if (n == 0) return cudaSuccess;
+  return cudaMallocAsync(p, n, st);
+}
+
+void dev_free(void* p, cudaStream_t st) {
+  if (p) cudaFreeAsync(p, st);
+}
+
+// Pinned host buffers are cached by power-of-two size and reused (cudaFreeHost
+// can synchronise the device too).
+std::mutex g_pin_mu;
+std::multimap<size_t, void*> g_pin_free;
+std::map<void*, size_t> g_pin_size;
+
+cudaError_t host_alloc(void** p, size_t n) {
+  size_t cls = 4096;
+  while (cls < n) cls <<= 1;
+  {
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    auto it = g_pin_free.find(cls);
+    if (it != g_pin_free.end()) {
+      *p = it->second;
+      g_pin_free.erase(it);
+      return cudaSuccess;
+    }
+  }
+  cudaError_t e = cudaMallocHost(p, cls);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  g_pin_size[*p] = cls;
+  return cudaSuccess;
+}
+
+void host_free(void* p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  auto it = g_pin_size.find(p);
+  if (it != g_pin_size.end()) g_pin_free.emplace(it->second, p);
+}
 
 }  // namespace
 
@@ -263,26 +328,27 @@ int ensure_capacity(lc2_context* c, int count) {
   if (count <= c->cap) return LC2_OK;
   drop_graphs(c);  // the graphs read the buffers being replaced
   int ncap = std::max(count, std::max(64, c->cap * 2));
-  if (c->d_xf) cudaFree(c->d_xf);
-  if (c->d_acc) cudaFree(c->d_acc);
-  if (c->d_out) cudaFree(c->d_out);
-  if (c->h_xf) cudaFreeHost(c->h_xf);
-  if (c->h_out) cudaFreeHost(c->h_out);
+  dev_free(c->d_xf, c->stream);
+  dev_free(c->d_acc, c->stream);
+  dev_free(c->d_out, c->stream);
+  if (c->h_xf || c->h_out) cudaStreamSynchronize(c->stream);  // pending copies
+  host_free(c->h_xf);
+  host_free(c->h_out);
   c->d_xf = nullptr; c->d_acc = nullptr; c->d_out = nullptr; c->h_xf = nullptr; c->h_out = nullptr;
   c->cap = 0;
-  LC2_CUDA(cudaMalloc(&c->d_xf, sizeof(lc2::Xform) * ncap));
-  LC2_CUDA(cudaMalloc(&c->d_acc, sizeof(unsigned long long) * 2 * ncap));
-  LC2_CUDA(cudaMalloc(&c->d_out, sizeof(double) * ncap));
-  LC2_CUDA(cudaMallocHost(&c->h_xf, sizeof(lc2::Xform) * ncap));
-  LC2_CUDA(cudaMallocHost(&c->h_out, sizeof(double) * ncap));
+  LC2_CUDA(dev_alloc((void**)&c->d_xf, sizeof(lc2::Xform) * ncap, c->stream));
+  LC2_CUDA(dev_alloc((void**)&c->d_acc, sizeof(unsigned long long) * 2 * ncap, c->stream));
+  LC2_CUDA(dev_alloc((void**)&c->d_out, sizeof(double) * ncap, c->stream));
+  LC2_CUDA(host_alloc((void**)&c->h_xf, sizeof(lc2::Xform) * ncap));
+  LC2_CUDA(host_alloc((void**)&c->h_out, sizeof(double) * ncap));
   if (c->mi) {
-    cudaFree(c->d_hist);
-    cudaFree(c->d_rmin);
-    cudaFree(c->d_rmax);
+    dev_free(c->d_hist, c->stream);
+    dev_free(c->d_rmin, c->stream);
+    dev_free(c->d_rmax, c->stream);
     c->d_hist = nullptr; c->d_rmin = nullptr; c->d_rmax = nullptr;
-    LC2_CUDA(cudaMalloc(&c->d_hist, sizeof(unsigned) * lc2::kMiHist * (size_t)ncap));
-    LC2_CUDA(cudaMalloc(&c->d_rmin, sizeof(unsigned) * ncap));
-    LC2_CUDA(cudaMalloc(&c->d_rmax, sizeof(unsigned) * ncap));
+    LC2_CUDA(dev_alloc((void**)&c->d_hist, sizeof(unsigned) * lc2::kMiHist * (size_t)ncap, c->stream));
+    LC2_CUDA(dev_alloc((void**)&c->d_rmin, sizeof(unsigned) * ncap, c->stream));
+    LC2_CUDA(dev_alloc((void**)&c->d_rmax, sizeof(unsigned) * ncap, c->stream));
   }
   c->cap = ncap;
   return LC2_OK;
@@ -674,27 +740,30 @@ int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
     return fail(LC2_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
   }
   c->stream = c->own_stream;
-  e = cudaMalloc(&c->d_scratch, c->per_slot * c->slots);
+  e = dev_alloc((void**)&c->d_scratch, c->per_slot * c->slots, c->stream);
   c->owns_moving = own_moving;
-  if (e == cudaSuccess && own_moving) e = cudaMalloc(&c->d_moving, c->nm * elem_size(cfg->storage));
+  if (e == cudaSuccess && own_moving) e = dev_alloc(&c->d_moving, c->nm * elem_size(cfg->storage), c->stream);
   if (e == cudaSuccess)
-    e = cudaMalloc(&c->d_static,
-                   c->nv * (cfg->high_res_is_moving ? elem_size(cfg->storage) : sizeof(float)));
+    e = dev_alloc(&c->d_static,
+                   c->nv * (cfg->high_res_is_moving ? elem_size(cfg->storage) : sizeof(float)), c->stream);
   if (e == cudaSuccess && !cfg->high_res_is_moving)
-    e = cudaMalloc(&c->d_gstatic, c->nv * sizeof(float));
+    e = dev_alloc((void**)&c->d_gstatic, c->nv * sizeof(float), c->stream);
   if (e == cudaSuccess && cfg->high_res_is_moving && !c->mi)
-    e = cudaMalloc(&c->d_sigma, c->nv * sizeof(float));
+    e = dev_alloc((void**)&c->d_sigma, c->nv * sizeof(float), c->stream);
   if (e == cudaSuccess && cfg->high_res_is_moving && !c->mi)
-    e = cudaMalloc(&c->d_su, c->nv * sizeof(int));
-  if (e == cudaSuccess && c->mi) e = cudaMalloc(&c->d_sbin, c->nv);
-  if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int));
-  if (e == cudaSuccess) e = cudaMallocHost(&c->h_err, sizeof(int));
-  if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(int));
+    e = dev_alloc((void**)&c->d_su, c->nv * sizeof(int), c->stream);
+  if (e == cudaSuccess && c->mi) e = dev_alloc((void**)&c->d_sbin, c->nv, c->stream);
+  if (e == cudaSuccess) e = dev_alloc((void**)&c->d_err, sizeof(int), c->stream);
+  if (e == cudaSuccess) e = host_alloc((void**)&c->h_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
   if (e != cudaSuccess) {
     lc2_destroy(c);
     return fail(LC2_ERR_OUT_OF_MEMORY, "device allocation: %s", cudaGetErrorString(e));
   }
   st = ensure_capacity(c, 64);
+  // the stream-ordered allocations are complete before any other stream uses them
+  if (st == LC2_OK && cudaStreamSynchronize(c->stream) != cudaSuccess)
+    st = fail(LC2_ERR_CUDA, "context allocation: %s", cudaGetErrorString(cudaGetLastError()));
   if (st != LC2_OK) {
     std::string msg = g_err;
     lc2_destroy(c);
@@ -729,24 +798,26 @@ int lc2_destroy(lc2_context* c) {
   if (!c) return LC2_OK;
   select_device(c);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  if (c->owns_moving) cudaFree(c->d_moving);
-  cudaFree(c->d_static);
-  cudaFree(c->d_gstatic);
-  cudaFree(c->d_sigma);
-  cudaFree(c->d_su);
-  cudaFree(c->d_err);
-  if (c->h_err) cudaFreeHost(c->h_err);
-  cudaFree(c->d_scratch);
   drop_graphs(c);
-  cudaFree(c->d_sbin);
-  cudaFree(c->d_hist);
-  cudaFree(c->d_rmin);
-  cudaFree(c->d_rmax);
-  cudaFree(c->d_xf);
-  cudaFree(c->d_acc);
-  cudaFree(c->d_out);
-  if (c->h_xf) cudaFreeHost(c->h_xf);
-  if (c->h_out) cudaFreeHost(c->h_out);
+  cudaStream_t fs = c->own_stream;  // frees are ordered on the context's own stream
+  if (c->owns_moving) dev_free(c->d_moving, fs);
+  dev_free(c->d_static, fs);
+  dev_free(c->d_gstatic, fs);
+  dev_free(c->d_sigma, fs);
+  dev_free(c->d_su, fs);
+  dev_free(c->d_err, fs);
+  dev_free(c->d_scratch, fs);
+  dev_free(c->d_sbin, fs);
+  dev_free(c->d_hist, fs);
+  dev_free(c->d_rmin, fs);
+  dev_free(c->d_rmax, fs);
+  dev_free(c->d_xf, fs);
+  dev_free(c->d_acc, fs);
+  dev_free(c->d_out, fs);
+  if (fs) cudaStreamSynchronize(fs);
+  host_free(c->h_err);
+  host_free(c->h_xf);
+  host_free(c->h_out);
   for (auto& t : c->timed) {
     cudaEventDestroy(t.a);
     cudaEventDestroy(t.b);
@@ -870,11 +941,12 @@ int image_absmax(const float* img, size_t n, const char* what, float* out) {
 // Host float image -> device buffer of the storage type (synchronous).
 int upload_image(lc2_context* c, const float* host, size_t n, void* dst, int storage) {
   float* tmp = nullptr;
-  LC2_CUDA(cudaMalloc(&tmp, sizeof(float) * n));
+  LC2_CUDA(dev_alloc((void**)&tmp, sizeof(float) * n, c->stream));
   struct Free {
     float* p;
-    ~Free() { cudaFree(p); }
-  } guard{tmp};
+    cudaStream_t st;
+    ~Free() { dev_free(p, st); }
+  } guard{tmp, c->stream};
   LC2_CUDA(cudaMemcpyAsync(tmp, host, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
   LC2_TRY(convert_to_storage(c, tmp, dst, n, storage));
   LC2_CUDA(cudaStreamSynchronize(c->stream));
@@ -959,13 +1031,14 @@ int set_fixed(lc2_context* c, const float* fixed, float fmax, float mmax) {
   const int storage = c->cfg.storage;
   struct Free {
     float* p;
-    ~Free() { cudaFree(p); }
+    cudaStream_t st;
+    ~Free() { dev_free(p, st); }
   };
   // fixed volume resampled onto the virtual grid through the identity
   // (VirtualToFixed, src/Interpolator/interpolator.cu:526-528)
   float* ffix = nullptr;
-  LC2_CUDA(cudaMalloc(&ffix, sizeof(float) * c->nf));
-  Free guard2{ffix};
+  LC2_CUDA(dev_alloc((void**)&ffix, sizeof(float) * c->nf, c->stream));
+  Free guard2{ffix, c->stream};
   LC2_CUDA(cudaMemcpyAsync(ffix, fixed, sizeof(float) * c->nf, cudaMemcpyHostToDevice, c->stream));
   lc2::Xform id{};
   {
@@ -1231,11 +1304,12 @@ int lc2_evaluate_fields(lc2_context* c, const float* matrix, double* lc2_out, fl
   const size_t nv = c->nv;
   float* osig = nullptr;
   float* omeas = nullptr;
-  LC2_CUDA(cudaMalloc(&osig, sizeof(float) * nv * 3));
+  LC2_CUDA(dev_alloc((void**)&osig, sizeof(float) * nv * 3, c->stream));
   struct Free {
     float* p;
-    ~Free() { cudaFree(p); }
-  } guard{osig};
+    cudaStream_t st;
+    ~Free() { dev_free(p, st); }
+  } guard{osig, c->stream};
   omeas = osig + nv;
   float* tmp = osig + 2 * nv;
   LC2_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2, c->stream));
@@ -1296,11 +1370,12 @@ int lc2_weighting_map(lc2_context* c, const float* matrix, double* lc2_out, floa
   LC2_TRY(select_device(c));
   const size_t nv = c->nv;
   float* buf = nullptr;
-  LC2_CUDA(cudaMalloc(&buf, sizeof(float) * nv * 3));
+  LC2_CUDA(dev_alloc((void**)&buf, sizeof(float) * nv * 3, c->stream));
   struct Free {
     float* p;
-    ~Free() { cudaFree(p); }
-  } guard{buf};
+    cudaStream_t st;
+    ~Free() { dev_free(p, st); }
+  } guard{buf, c->stream};
   float* osig = buf;
   float* omeas = buf + nv;
   float* dmap = buf + 2 * nv;
@@ -1481,15 +1556,16 @@ void stack_drop_graphs(lc2_stack* s) {
 }
 
 void stack_free_buffers(lc2_stack* s) {
-  cudaFree(s->d_xf);
-  cudaFree(s->d_acc);
-  cudaFree(s->d_sums);
-  cudaFree(s->d_out);
-  cudaFree(s->d_segs);
-  if (s->h_xf) cudaFreeHost(s->h_xf);
-  if (s->h_sums) cudaFreeHost(s->h_sums);
-  if (s->h_out) cudaFreeHost(s->h_out);
-  if (s->h_segs) cudaFreeHost(s->h_segs);
+  dev_free(s->d_xf, s->stream);
+  dev_free(s->d_acc, s->stream);
+  dev_free(s->d_sums, s->stream);
+  dev_free(s->d_out, s->stream);
+  dev_free(s->d_segs, s->stream);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  host_free(s->h_xf);
+  host_free(s->h_sums);
+  host_free(s->h_out);
+  host_free(s->h_segs);
   s->d_xf = nullptr; s->d_acc = nullptr; s->d_sums = nullptr; s->d_out = nullptr;
   s->d_segs = nullptr; s->h_xf = nullptr; s->h_sums = nullptr; s->h_out = nullptr;
   s->h_segs = nullptr;
@@ -1504,15 +1580,15 @@ int stack_capacity(lc2_stack* s, int count, int nseg) {
   const int ncap = std::max(count, std::max(256, s->cap));
   const int nseg_cap = std::max(nseg, std::max(64, s->seg_cap));
   stack_free_buffers(s);
-  LC2_CUDA(cudaMalloc(&s->d_xf, sizeof(lc2::Xform) * ncap));
-  LC2_CUDA(cudaMalloc(&s->d_acc, sizeof(unsigned long long) * 2 * ncap));
-  LC2_CUDA(cudaMalloc(&s->d_sums, sizeof(long long) * ncap));
-  LC2_CUDA(cudaMalloc(&s->d_out, sizeof(double) * ncap));
-  LC2_CUDA(cudaMalloc(&s->d_segs, sizeof(lc2::ListSeg) * nseg_cap));
-  LC2_CUDA(cudaMallocHost(&s->h_xf, sizeof(lc2::Xform) * ncap));
-  LC2_CUDA(cudaMallocHost(&s->h_sums, sizeof(long long) * ncap));
-  LC2_CUDA(cudaMallocHost(&s->h_out, sizeof(double) * ncap));
-  LC2_CUDA(cudaMallocHost(&s->h_segs, sizeof(lc2::ListSeg) * nseg_cap));
+  LC2_CUDA(dev_alloc((void**)&s->d_xf, sizeof(lc2::Xform) * ncap, s->stream));
+  LC2_CUDA(dev_alloc((void**)&s->d_acc, sizeof(unsigned long long) * 2 * ncap, s->stream));
+  LC2_CUDA(dev_alloc((void**)&s->d_sums, sizeof(long long) * ncap, s->stream));
+  LC2_CUDA(dev_alloc((void**)&s->d_out, sizeof(double) * ncap, s->stream));
+  LC2_CUDA(dev_alloc((void**)&s->d_segs, sizeof(lc2::ListSeg) * nseg_cap, s->stream));
+  LC2_CUDA(host_alloc((void**)&s->h_xf, sizeof(lc2::Xform) * ncap));
+  LC2_CUDA(host_alloc((void**)&s->h_sums, sizeof(long long) * ncap));
+  LC2_CUDA(host_alloc((void**)&s->h_out, sizeof(double) * ncap));
+  LC2_CUDA(host_alloc((void**)&s->h_segs, sizeof(lc2::ListSeg) * nseg_cap));
   s->cap = ncap;
   s->seg_cap = nseg_cap;
   return LC2_OK;
@@ -1587,7 +1663,7 @@ int lc2_stack_create(const lc2_geometry* moving, int patch_size, int storage, in
   cudaError_t e = cudaSuccess;
   if (st == LC2_OK) e = cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, device);
   if (st == LC2_OK && e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
-  if (st == LC2_OK && e == cudaSuccess) e = cudaMalloc(&s->d_moving, s->nm * elem_size(storage));
+  if (st == LC2_OK && e == cudaSuccess) e = dev_alloc(&s->d_moving, s->nm * elem_size(storage), s->stream);
   if (st != LC2_OK || e != cudaSuccess) {
     std::string msg = st != LC2_OK ? g_err : std::string(cudaGetErrorString(e));
     lc2_stack_destroy(s);
@@ -1604,8 +1680,11 @@ int lc2_stack_destroy(lc2_stack* s) {
   for (lc2_context* f : s->frames) lc2_destroy(f);
   stack_drop_graphs(s);
   stack_free_buffers(s);
-  cudaFree(s->d_moving);
-  if (s->stream) cudaStreamDestroy(s->stream);
+  dev_free(s->d_moving, s->stream);
+  if (s->stream) {
+    cudaStreamSynchronize(s->stream);
+    cudaStreamDestroy(s->stream);
+  }
   delete s;
   return LC2_OK;
 }
@@ -1619,11 +1698,12 @@ int lc2_stack_set_moving(lc2_stack* s, const float* moving) {
   LC2_TRY(image_absmax(moving, s->nm, "moving", &mmax));
   // staged through a temporary one-slot context for its conversion kernels
   float* tmp = nullptr;
-  LC2_CUDA(cudaMalloc(&tmp, sizeof(float) * s->nm));
+  LC2_CUDA(dev_alloc((void**)&tmp, sizeof(float) * s->nm, s->stream));
   struct Free {
     float* p;
-    ~Free() { cudaFree(p); }
-  } guard{tmp};
+    cudaStream_t st;
+    ~Free() { dev_free(p, st); }
+  } guard{tmp, s->stream};
   LC2_CUDA(cudaMemcpyAsync(tmp, moving, sizeof(float) * s->nm, cudaMemcpyHostToDevice, s->stream));
   lc2_context conv;  // only its stream and launch counter are used
   conv.stream = s->stream;
