@@ -542,11 +542,17 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
     const int zb = blockIdx.z * P.zchunk;
     const int ze = min(zb + P.zchunk, P.vz);
     constexpr int MAXP = G::MAXP, WP = G::WP;
-    int acc32[MAXP][kLimbs];
+    // z-window sums of each halo point: qM, qG exactly in int32, the five
+    // products in int64 (split into hi * 2^K + lo limbs only when written)
+    int accq[MAXP][2];
+    long long accp[MAXP][5];
 #pragma unroll
-    for (int j = 0; j < MAXP; ++j)
+    for (int j = 0; j < MAXP; ++j) {
+      accq[j][0] = accq[j][1] = 0;
 #pragma unroll
-      for (int k = 0; k < kLimbs; ++k) acc32[j][k] = 0;
+      for (int k = 0; k < 5; ++k) accp[j][k] = 0;
+    }
+    const unsigned long long kmask = (1ull << P.kbits) - 1ull;
     // per-thread constants of its halo points: plane index, A offset, U offset
     int pc[MAXP], pa_off[MAXP], pu[MAXP];
     bool pin[MAXP];
@@ -663,25 +669,37 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* 
           const float m = mc[pc[j]];
           const float g = fused_sobel_sd<G::PW>(SD, pc[j]);
           const int qm = quant(m, P.qm), qg = quant(g, P.qg), qu = quant(u_in[j], P.qu);
-          int Li[kLimbs];
-          fused_limbs(qu, qm, qg, P.kbits, Li);
           lv_in[p] = qm;
           lv_in[G::NP + p] = qg;
           if constexpr (G::RINGW == 3) lv_in[2 * G::NP + p] = qu;
+          long long pin5[5] = {(long long)qu * qm, (long long)qu * qg, (long long)qm * qm,
+                               (long long)qg * qg, (long long)qm * qg};
+          int dqm = qm, dqg = qg;
           if (leave) {
-            int Lo[kLimbs];
             const int qul = (G::RINGW == 3) ? lv_out[2 * G::NP + p] : quant(u_out[j], P.qu);
-            fused_limbs(qul, lv_out[p], lv_out[G::NP + p], P.kbits, Lo);
-#pragma unroll
-            for (int k = 0; k < kLimbs; ++k) acc32[j][k] += Li[k] - Lo[k];
-          } else {
-#pragma unroll
-            for (int k = 0; k < kLimbs; ++k) acc32[j][k] += Li[k];
+            const int qml = lv_out[p], qgl = lv_out[G::NP + p];
+            pin5[0] -= (long long)qul * qml;
+            pin5[1] -= (long long)qul * qgl;
+            pin5[2] -= (long long)qml * qml;
+            pin5[3] -= (long long)qgl * qgl;
+            pin5[4] -= (long long)qml * qgl;
+            dqm -= qml;
+            dqg -= qgl;
           }
-          if (out) {
-            int* a = A + pa_off[j];
+          accq[j][0] += dqm;
+          accq[j][1] += dqg;
 #pragma unroll
-            for (int k = 0; k < kLimbs; ++k) a[k * PA] = acc32[j][k];
+          for (int k = 0; k < 5; ++k) accp[j][k] += pin5[k];
+          if (out) {
+            // the same limb layout as fused_limbs: qM, qG, then (lo, hi) per product
+            int* a = A + pa_off[j];
+            a[0] = accq[j][0];
+            a[PA] = accq[j][1];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+              a[(2 + 2 * k) * PA] = (int)((unsigned long long)accp[j][k] & kmask);
+              a[(3 + 2 * k) * PA] = (int)(accp[j][k] >> P.kbits);
+            }
           }
         }
       }
