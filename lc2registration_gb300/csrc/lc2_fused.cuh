@@ -446,7 +446,7 @@ __device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
 }
 
 template <int ND, int WND, typename TM, typename TS, int TY, int R>
-__global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : 1) k_fused(const TM* __restrict__ mov,
+__global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : (ND == 2 ? 4 : 1)) k_fused(const TM* __restrict__ mov,
                                                       const TS* __restrict__ Ust,
                                                       const float* __restrict__ sig,
                                                       const int* __restrict__ su,

@@ -32,7 +32,7 @@ struct ListSeg {
 constexpr int kListTY = 16;
 
 template <int WND, typename T, int R>
-__global__ void __launch_bounds__(32 * kListTY, 1)
+__global__ void __launch_bounds__(32 * kListTY, 3)
     k_fused_list(const ListSeg* __restrict__ segs, int nseg, long long units,
                  const Xform* __restrict__ xf, unsigned long long* __restrict__ acc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
