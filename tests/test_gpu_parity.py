@@ -34,6 +34,10 @@ def _case(kind):
     if kind == "3d_r4":
         return synth.case_3d(seed=23, mr_size=48, us_size=40, r=4, blobs=6, blur=1.5,
                              constant_block_frac=0.1)
+    if kind == "3d_r5":  # largest radii: 8-row tiles
+        return synth.case_3d(seed=24, mr_size=44, us_size=36, r=5, blobs=6, blur=1.5)
+    if kind == "3d_r6":
+        return synth.case_3d(seed=25, mr_size=44, us_size=36, r=6, blobs=6, blur=1.5)
     if kind == "2dto3d":
         mr = synth.mr_phantom((40, 40, 40), 6, 1.5, seed=31)
         mg = Geometry((40, 40, 40), (1, 1, 1), (0, 0, 0))
@@ -51,7 +55,7 @@ def _hr_fixed(case):
     return c
 
 
-CASES = ["2d", "2d_r1", "2d_r9", "3d", "3d_r3", "3d_r4", "2dto3d"]
+CASES = ["2d", "2d_r1", "2d_r9", "3d", "3d_r3", "3d_r4", "3d_r5", "3d_r6", "2dto3d"]
 
 
 @pytest.mark.parametrize("kind", CASES)
@@ -213,3 +217,24 @@ def test_fields_match_reference_kernels(name):
     S = ref["S"].astype(np.float64)
     close = np.abs(S - f["measure"]) <= 1e-4 * np.maximum(w, 1e-12)
     assert close[both].mean() > 0.975
+
+
+@pytest.mark.parametrize("kind", ["2d", "3d"])
+def test_degenerate_inputs(kind):
+    """Edge cases with known answers: a constant ultrasound has no valid
+    patch (every sigma is 0, LC2 = 0/0 -> 0), and a transform that maps the
+    whole virtual grid outside the moving image leaves M = G = 0 (no measure,
+    LC2 = 0), on the GPU as in the oracle."""
+    case = _case(kind)
+    flat = synth.Case(case.mode, case.fixed_geom, np.full_like(case.fixed, 0.7),
+                      case.moving_geom, case.moving, case.virt_spacing, case.r, case.hr_moving,
+                      case.true_params, case.true_mat)
+    ctx = make_context(flat)
+    assert ctx.evaluate(flat.true_mat) == 0.0
+    assert oracle_eval(flat, flat.true_mat) == 0.0
+    away = case.true_mat.copy()
+    away[0, -1] += 1e4  # translate far outside the moving image
+    ctx2 = make_context(case)
+    assert ctx2.evaluate(away) == 0.0
+    assert oracle_eval(case, away) == 0.0
+    np.testing.assert_array_equal(ctx2.evaluate_batch(np.stack([away, away])), [0.0, 0.0])
