@@ -308,6 +308,7 @@ void build_xform(int nd, const lc2_geometry& v, const lc2_geometry& m, const flo
     X->A[2] = 0.0;
     X->A[5] = 0.0;
   }
+  lc2::xform_split(*X);
 }
 
 long long floor_clamp(long double v) {

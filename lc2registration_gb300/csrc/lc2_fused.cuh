@@ -315,8 +315,7 @@ __device__ __forceinline__ float fused_sobel_sd(const float2* SD, int c) {
 
 // Per-tile transform state in shared memory.
 struct TileShared {
-  double base[3];  // resampled-region origin in moving pixels
-  int ib[3];       // its integer part
+  int ib[3];       // resampled-region origin in moving pixels: integer part
   float fb[3];     // and fraction
   float A[9];      // moving-pixel step per region pixel
   int inside;      // every sample of the region lies strictly inside the moving image
@@ -365,15 +364,9 @@ __device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
   const int gx0 = x0 - R - 1, gy0 = y0 - R - 1;
   if (tid == 0) {
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const double p = X->A[3 * a + 0] * gx0 + X->A[3 * a + 1] * gy0 + X->b[a];
-      const double fl = floor(p);
-      T.base[a] = p;
-      T.ib[a] = (int)fl;
-      T.fb[a] = (float)(p - fl);
-    }
+    for (int a = 0; a < 3; ++a) xform_coord(X->s, a, gx0, gy0, 0, T.ib[a], T.fb[a]);
 #pragma unroll
-    for (int i = 0; i < 9; ++i) T.A[i] = (float)X->A[i];
+    for (int i = 0; i < 9; ++i) T.A[i] = X->s.ah[i];
     // region in the virtual grid and every sample strictly inside the moving
     // image (corners bound the affine image; 0.01 voxel covers float rounding)
     bool in = gx0 >= 0 && gx0 + G::PW <= P.vx && gy0 >= 0 && gy0 + G::PH <= P.vy;
@@ -445,15 +438,17 @@ __device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
   return acc_m;
 }
 
+// CTAs per SM each variant is compiled for: 2D tiles 4; 3D 16-row tiles 1;
+// 3D 8-row tiles 2 up to radius 4 (beyond, shared memory holds only one).
+constexpr int fused_min_blocks(int nd, int ty, int r) {
+  return nd == 2 ? 4 : (ty == 8 && r <= 4 ? 2 : 1);
+}
+
 template <int ND, int WND, typename TM, typename TS, int TY, int R>
-__global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : (ND == 2 ? 4 : 1)) k_fused(const TM* __restrict__ mov,
-                                                      const TS* __restrict__ Ust,
-                                                      const float* __restrict__ sig,
-                                                      const int* __restrict__ su,
-                                                      FusedParams P,
-                                                      const Xform* __restrict__ xf, int k0,
-                                                      unsigned long long* __restrict__ acc,
-                                                      float* __restrict__ out_measure) {
+__global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
+    k_fused(const TM* __restrict__ mov, const TS* __restrict__ Ust, const float* __restrict__ sig,
+            const int* __restrict__ su, FusedParams P, const Xform* __restrict__ xf, int k0,
+            unsigned long long* __restrict__ acc, float* __restrict__ out_measure) {
   using G = FusedGeom<ND, TY, R>;
   constexpr int NT = G::NT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -462,7 +457,7 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : (ND == 2 ? 4 : 1)) k_
   int* lv = reinterpret_cast<int*>(smem_raw + G::OFF_LV);
   int* A = reinterpret_cast<int*>(smem_raw + G::OFF_A);
   constexpr size_t PA = (size_t)G::HY * G::HXP;
-  __shared__ double s_base[3];
+  __shared__ XformSplit s_xf;
   __shared__ int s_ib[3];
   __shared__ float s_fb[3];
   __shared__ float s_A[9];
@@ -481,10 +476,11 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : (ND == 2 ? 4 : 1)) k_
   const int ox = tid & 31, oy = tid >> 5;
   long long acc_m = 0;
 
-  // thread 0: sampling base at slice zs in double, split into integer part
-  // and fraction for the float per-point offsets
+  // sampling base at slice zs (xform_coord), split into integer part and
+  // fraction for the float per-point offsets; run by the last thread, whose
+  // warp holds the fewest halo points
   auto set_base = [&](int zs) {
-    if (tid == 0) {
+    if (tid == NT - 1) {
       // the region lies in the virtual grid and every sample of it strictly
       // inside the moving volume (0 <= floor, floor + 1 <= dim - 1; corners of
       // the region bound the affine image, 0.01 voxel covers float rounding)
@@ -493,10 +489,7 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : (ND == 2 ? 4 : 1)) k_
       const int dims[3] = {P.mx, P.my, P.mz};
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        double p = s_base[a] + X->A[3 * a + 2] * (double)zs;
-        double fl = floor(p);
-        s_ib[a] = (int)fl;
-        s_fb[a] = (float)(p - fl);
+        xform_coord(s_xf, a, gx0, gy0 - yb, zs, s_ib[a], s_fb[a]);
         const float ex = s_A[3 * a] * (float)(G::PW - 1);
         const float e0 = s_A[3 * a + 1] * (float)yb, e1 = s_A[3 * a + 1] * (float)(yb + G::PH - 1);
         const float lo = s_fb[a] + fminf(ex, 0.0f) + fminf(e0, e1);
@@ -507,11 +500,9 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : (ND == 2 ? 4 : 1)) k_
     }
   };
   if (tid == 0) {
+    s_xf = X->s;
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
-      s_base[a] = X->A[3 * a + 0] * gx0 + X->A[3 * a + 1] * (gy0 - yb) + X->b[a];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) s_A[i] = (float)X->A[i];
+    for (int i = 0; i < 9; ++i) s_A[i] = X->s.ah[i];
   }
 
   // solve one output voxel from the patch sums in A rows < TY
@@ -626,6 +617,7 @@ __global__ void __launch_bounds__(32 * TY, (TY == 8) ? 2 : (ND == 2 ? 4 : 1)) k_
         out[k] = v;
       }
     };
+    __syncthreads();  // s_xf, s_A
     set_base(e0 - 1);
     __syncthreads();
     warp_slice(e0 - 1, m_prev2);

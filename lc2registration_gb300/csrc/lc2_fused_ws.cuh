@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(WsGeom<R>::NT, 1)
   int* lv = reinterpret_cast<int*>(smem_raw + W::OFF_LV);
   int* A = reinterpret_cast<int*>(smem_raw + W::OFF_A);
   __shared__ __align__(8) unsigned long long full[kWsSlots], empty[kWsSlots];
-  __shared__ double s_base[3], s_az[3];
+  __shared__ XformSplit s_xf;
   __shared__ float s_A[9];
   __shared__ volatile int s_abort;
 
@@ -124,44 +124,25 @@ __global__ void __launch_bounds__(WsGeom<R>::NT, 1)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
+    s_xf = X->s;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      s_base[a] = X->A[3 * a + 0] * gx0 + X->A[3 * a + 1] * (gy0 - yb) + X->b[a];
-      s_az[a] = X->A[3 * a + 2];
-    }
-#pragma unroll
-    for (int i = 0; i < 9; ++i) s_A[i] = (float)X->A[i];
+    for (int i = 0; i < 9; ++i) s_A[i] = X->s.ah[i];
     s_abort = 0;
   }
   __syncthreads();
 
   if (tid >= NC) {
     // ------------------------------------------------------------ producers
-    const int ptid = tid - NC, lane = tid & 31;
+    const int ptid = tid - NC;
     for (int q = 0; q < nslices; ++q) {
       const int sl = q % kWsSlots, use = q / kWsSlots;
       if (use > 0) mbar_wait(&empty[sl], (unsigned)((use - 1) & 1), &s_abort, err);
       const int zs = e0 - 1 + q;
-      // base of slice zs: lane 0 of each warp in double, broadcast
+      // base of slice zs (every lane computes the same value)
       int ib[3];
       float fb[3];
-      {
-        int i0 = 0, i1 = 0, i2 = 0;
-        float f0 = 0.f, f1 = 0.f, f2 = 0.f;
-        if (lane == 0) {
-          double p0 = s_base[0] + s_az[0] * (double)zs, p1 = s_base[1] + s_az[1] * (double)zs,
-                 p2 = s_base[2] + s_az[2] * (double)zs;
-          double l0 = floor(p0), l1 = floor(p1), l2 = floor(p2);
-          i0 = (int)l0; i1 = (int)l1; i2 = (int)l2;
-          f0 = (float)(p0 - l0); f1 = (float)(p1 - l1); f2 = (float)(p2 - l2);
-        }
-        ib[0] = __shfl_sync(0xffffffffu, i0, 0);
-        ib[1] = __shfl_sync(0xffffffffu, i1, 0);
-        ib[2] = __shfl_sync(0xffffffffu, i2, 0);
-        fb[0] = __shfl_sync(0xffffffffu, f0, 0);
-        fb[1] = __shfl_sync(0xffffffffu, f1, 0);
-        fb[2] = __shfl_sync(0xffffffffu, f2, 0);
-      }
+#pragma unroll
+      for (int a = 0; a < 3; ++a) xform_coord(s_xf, a, gx0, gy0 - yb, zs, ib[a], fb[a]);
       float* out = ring + (size_t)sl * G::NPW;
       const bool zin = (zs >= 0 && zs < P.vz);
       for (int i = ptid; i < G::NPW; i += kWsProducers) {

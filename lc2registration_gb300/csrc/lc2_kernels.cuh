@@ -64,10 +64,81 @@ __device__ __forceinline__ __nv_bfloat16 stf<__nv_bfloat16>(float v) {
 // Moving-pixel coordinates of virtual voxel (x, y, z): p = A (x, y, z) + b.
 // Built on the host in double from the row-major mm matrix and the three
 // geometries: A = diag(1/spM) L diag(spV), b = diag(1/spM) (L oV + t - oM).
+// The kernels read only the float-float split (hi + lo) of A and b, made by
+// xform_split on the host: hi carries 24 bits, lo the next 24.
+struct XformSplit {
+  float ah[9], al[9];
+  float bh[3], bl[3];
+};
+
 struct Xform {
   double A[9];
   double b[3];
+  XformSplit s;
 };
+
+// Host: fill X.s from X.A and X.b.
+inline void xform_split(Xform& X) {
+  for (int i = 0; i < 9; ++i) {
+    X.s.ah[i] = (float)X.A[i];
+    X.s.al[i] = (float)(X.A[i] - (double)X.s.ah[i]);
+  }
+  for (int a = 0; a < 3; ++a) {
+    X.s.bh[a] = (float)X.b[a];
+    X.s.bl[a] = (float)(X.b[a] - (double)X.s.bh[a]);
+  }
+}
+
+// s + e = a + b exactly (Knuth's two-sum); explicit round-to-nearest
+// intrinsics keep the compiler from contracting or reordering the steps.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Moving-pixel coordinate p = A (x, y, z) + b of virtual voxel (x, y, z)
+// along axis a, split into integer part ib and fraction fb in [0, 1).
+// Evaluated in float-float without double arithmetic (the FP64 pipe is
+// narrow on this part): the products of the hi coefficients are exact
+// (value + fma residual), the partial sums error-free (two-sum), so p keeps
+// about 48 significant bits -- far below the float fraction's rounding.
+// Integer parts are clamped to +-2^30 voxels, outside any volume.
+__device__ __forceinline__ void xform_coord(const XformSplit& X, int a, int x, int y, int z,
+                                            int& ib, float& fb) {
+  const float fx = (float)x, fy = (float)y, fz = (float)z;  // exact: |x| < 2^24
+  const float h0 = X.ah[3 * a], h1 = X.ah[3 * a + 1], h2 = X.ah[3 * a + 2];
+  const float p0 = __fmul_rn(h0, fx), p1 = __fmul_rn(h1, fy), p2 = __fmul_rn(h2, fz);
+  float err = __fmaf_rn(h0, fx, -p0);
+  err = __fadd_rn(err, __fmaf_rn(h1, fy, -p1));
+  err = __fadd_rn(err, __fmaf_rn(h2, fz, -p2));
+  err = __fmaf_rn(X.al[3 * a], fx, err);
+  err = __fmaf_rn(X.al[3 * a + 1], fy, err);
+  err = __fmaf_rn(X.al[3 * a + 2], fz, err);
+  err = __fadd_rn(err, X.bl[a]);
+  float s = X.bh[a], e;
+  two_sum(s, p0, s, e);
+  err = __fadd_rn(err, e);
+  two_sum(s, p1, s, e);
+  err = __fadd_rn(err, e);
+  two_sum(s, p2, s, e);
+  err = __fadd_rn(err, e);
+  float hi, lo;
+  two_sum(s, err, hi, lo);
+  float fl = floorf(hi);
+  float fr = __fadd_rn(__fsub_rn(hi, fl), lo);  // hi - fl is exact
+  if (fr < 0.0f) {
+    fr = __fadd_rn(fr, 1.0f);
+    fl = __fsub_rn(fl, 1.0f);
+  }
+  if (fr >= 1.0f) {  // p within half an ulp below an integer
+    fr = __fsub_rn(fr, 1.0f);
+    fl = __fadd_rn(fl, 1.0f);
+  }
+  fl = fminf(fmaxf(fl, -1073741824.0f), 1073741824.0f);  // NaN -> -2^30
+  ib = (int)fl;
+  fb = fr;
+}
 
 // ---------------------------------------------------------------------------
 // Resampling
@@ -93,7 +164,7 @@ __device__ __forceinline__ Axis make_axis(int base, float q, int dim) {
 }
 
 // Tile base of a 32 x 8 tile (x0, y0) of slice z: the moving-pixel
-// coordinate in double, split into integer part and fraction, plus the float
+// coordinate split into integer part and fraction (xform_coord), plus the float
 // step matrix. Each voxel adds a float offset of at most (31, 7) voxels to the
 // base fraction, so the interpolation weights keep ~1e-6 voxel accuracy
 // anywhere in the grid.
@@ -105,14 +176,9 @@ struct TileBase {
 
 __device__ __forceinline__ void tile_base(const Xform* X, int x0, int y0, int z, TileBase& T) {
 #pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    double p = X->A[3 * a + 0] * x0 + X->A[3 * a + 1] * y0 + X->A[3 * a + 2] * z + X->b[a];
-    double fl = floor(p);
-    T.ib[a] = (int)fl;
-    T.fb[a] = (float)(p - fl);
-  }
+  for (int a = 0; a < 3; ++a) xform_coord(X->s, a, x0, y0, z, T.ib[a], T.fb[a]);
 #pragma unroll
-  for (int i = 0; i < 9; ++i) T.A[i] = (float)X->A[i];
+  for (int i = 0; i < 9; ++i) T.A[i] = X->s.ah[i];
 }
 
 // Trilinear (ND = 3) / bilinear (ND = 2) sample at offset (tx, ty) from the

@@ -177,6 +177,7 @@ extern "C" int lc2_evaluate_noalloc(int mode, const lc2_geometry* virt, const lc
       }
       xf.b[a] = (a < warp_nd) ? bs / (double)moving->spacing[a] : 0.0;
     }
+    lc2::xform_split(xf);
   }
   NA_CUDA(cudaMemcpyAsync(&hdr->xf, &xf, sizeof(xf), cudaMemcpyHostToDevice, stream));
 
