@@ -472,6 +472,22 @@ def main():
     except Exception:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
+    # the reference's own kernels on this GPU type, measured separately by
+    # oracle/ref_golden/ref_gpu_time.py (profiles/reference_gpu_kernels.md)
+    ref_gpu = None
+    rfile = os.path.join(ROOT, "profiles", "reference_gpu_kernels.json")
+    if os.path.exists(rfile):
+        try:
+            ref_rows = {w["workload"]: w for w in json.load(open(rfile))}
+            row = ref_rows.get(f"3d_{args.size}_r{args.patch}")
+            if row:
+                ref_gpu = {"ms_per_eval": row["ms_per_eval"],
+                           "evals_per_s": 1e3 / row["ms_per_eval"], "storage": "f32",
+                           "lc2": row["lc2"],
+                           "source": "profiles/reference_gpu_kernels.json (one plain evaluation "
+                                     "of the reference's kernels, CUDA events, same GPU type)"}
+        except Exception:
+            ref_gpu = None
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "k_fused_traffic.json")
     if os.path.exists(tfile):
@@ -538,6 +554,7 @@ def main():
                     "d2h_bytes_per_step": K * 8},
             "plain": {"value": plain_eps, "unit": UNIT, "evals": P,
                       "batched_over_plain": value / world / plain_eps},
+            "reference_gpu_kernels": ref_gpu,
             "small_configs": small,
             "stack": stack,
             "serve": serve,

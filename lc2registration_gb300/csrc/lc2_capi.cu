@@ -276,7 +276,8 @@ bool finite_geom(const lc2_geometry& g) {
   return true;
 }
 
-// Moving-pixel affine of virtual voxels (see lc2::Xform).
+// Moving-pixel affine of virtual voxels in double (lc2::XformD), stored as
+// the float-float split the kernels read (lc2::Xform).
 void build_xform(int nd, const lc2_geometry& v, const lc2_geometry& m, const float* mat,
                  lc2::Xform* X) {
   double L[3][3] = {{0}}, t[3] = {0};
@@ -292,23 +293,24 @@ void build_xform(int nd, const lc2_geometry& v, const lc2_geometry& m, const flo
       t[a] = mat[4 * a + 3];
     }
   }
+  lc2::XformD D{};
   for (int a = 0; a < 3; ++a) {
     double bsum = t[a] - (double)m.origin[a];
     for (int b = 0; b < 3; ++b) {
-      X->A[3 * a + b] = L[a][b] * (double)v.spacing[b] / (double)m.spacing[a];
+      D.A[3 * a + b] = L[a][b] * (double)v.spacing[b] / (double)m.spacing[a];
       bsum += L[a][b] * (double)v.origin[b];
     }
-    X->b[a] = bsum / (double)m.spacing[a];
+    D.b[a] = bsum / (double)m.spacing[a];
     if (nd == 2 && a == 2) {
-      X->A[6] = X->A[7] = X->A[8] = 0.0;
-      X->b[2] = 0.0;
+      D.A[6] = D.A[7] = D.A[8] = 0.0;
+      D.b[2] = 0.0;
     }
   }
   if (nd == 2) {
-    X->A[2] = 0.0;
-    X->A[5] = 0.0;
+    D.A[2] = 0.0;
+    D.A[5] = 0.0;
   }
-  lc2::xform_split(*X);
+  *X = lc2::xform_split(D);
 }
 
 long long floor_clamp(long double v) {

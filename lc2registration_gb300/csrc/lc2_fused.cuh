@@ -364,9 +364,9 @@ __device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
   const int gx0 = x0 - R - 1, gy0 = y0 - R - 1;
   if (tid == 0) {
 #pragma unroll
-    for (int a = 0; a < 3; ++a) xform_coord(X->s, a, gx0, gy0, 0, T.ib[a], T.fb[a]);
+    for (int a = 0; a < 3; ++a) xform_coord(*X, a, gx0, gy0, 0, T.ib[a], T.fb[a]);
 #pragma unroll
-    for (int i = 0; i < 9; ++i) T.A[i] = X->s.ah[i];
+    for (int i = 0; i < 9; ++i) T.A[i] = X->ah[i];
     // region in the virtual grid and every sample strictly inside the moving
     // image (corners bound the affine image; 0.01 voxel covers float rounding)
     bool in = gx0 >= 0 && gx0 + G::PW <= P.vx && gy0 >= 0 && gy0 + G::PH <= P.vy;
@@ -457,7 +457,7 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
   int* lv = reinterpret_cast<int*>(smem_raw + G::OFF_LV);
   int* A = reinterpret_cast<int*>(smem_raw + G::OFF_A);
   constexpr size_t PA = (size_t)G::HY * G::HXP;
-  __shared__ XformSplit s_xf;
+  __shared__ Xform s_xf;
   __shared__ int s_ib[3];
   __shared__ float s_fb[3];
   __shared__ float s_A[9];
@@ -500,9 +500,9 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
     }
   };
   if (tid == 0) {
-    s_xf = X->s;
+    s_xf = *X;
 #pragma unroll
-    for (int i = 0; i < 9; ++i) s_A[i] = X->s.ah[i];
+    for (int i = 0; i < 9; ++i) s_A[i] = X->ah[i];
   }
 
   // solve one output voxel from the patch sums in A rows < TY

@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(WsGeom<R>::NT, 1)
   int* lv = reinterpret_cast<int*>(smem_raw + W::OFF_LV);
   int* A = reinterpret_cast<int*>(smem_raw + W::OFF_A);
   __shared__ __align__(8) unsigned long long full[kWsSlots], empty[kWsSlots];
-  __shared__ XformSplit s_xf;
+  __shared__ Xform s_xf;
   __shared__ float s_A[9];
   __shared__ volatile int s_abort;
 
@@ -124,9 +124,9 @@ __global__ void __launch_bounds__(WsGeom<R>::NT, 1)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    s_xf = X->s;
+    s_xf = *X;
 #pragma unroll
-    for (int i = 0; i < 9; ++i) s_A[i] = X->s.ah[i];
+    for (int i = 0; i < 9; ++i) s_A[i] = X->ah[i];
     s_abort = 0;
   }
   __syncthreads();

@@ -64,29 +64,31 @@ __device__ __forceinline__ __nv_bfloat16 stf<__nv_bfloat16>(float v) {
 // Moving-pixel coordinates of virtual voxel (x, y, z): p = A (x, y, z) + b.
 // Built on the host in double from the row-major mm matrix and the three
 // geometries: A = diag(1/spM) L diag(spV), b = diag(1/spM) (L oV + t - oM).
-// The kernels read only the float-float split (hi + lo) of A and b, made by
-// xform_split on the host: hi carries 24 bits, lo the next 24.
-struct XformSplit {
+struct XformD {
+  double A[9];
+  double b[3];
+};
+
+// What the kernels read: the float-float split (hi + lo) of A and b; hi
+// carries the first 24 significant bits, lo the next 24. 96 bytes.
+struct Xform {
   float ah[9], al[9];
   float bh[3], bl[3];
 };
+static_assert(sizeof(Xform) == 96, "one transform is staged host->device as 96 bytes");
 
-struct Xform {
-  double A[9];
-  double b[3];
-  XformSplit s;
-};
-
-// Host: fill X.s from X.A and X.b.
-inline void xform_split(Xform& X) {
+// Host: the split of D.
+inline Xform xform_split(const XformD& D) {
+  Xform X;
   for (int i = 0; i < 9; ++i) {
-    X.s.ah[i] = (float)X.A[i];
-    X.s.al[i] = (float)(X.A[i] - (double)X.s.ah[i]);
+    X.ah[i] = (float)D.A[i];
+    X.al[i] = (float)(D.A[i] - (double)X.ah[i]);
   }
   for (int a = 0; a < 3; ++a) {
-    X.s.bh[a] = (float)X.b[a];
-    X.s.bl[a] = (float)(X.b[a] - (double)X.s.bh[a]);
+    X.bh[a] = (float)D.b[a];
+    X.bl[a] = (float)(D.b[a] - (double)X.bh[a]);
   }
+  return X;
 }
 
 // s + e = a + b exactly (Knuth's two-sum); explicit round-to-nearest
@@ -104,7 +106,7 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 // (value + fma residual), the partial sums error-free (two-sum), so p keeps
 // about 48 significant bits -- far below the float fraction's rounding.
 // Integer parts are clamped to +-2^30 voxels, outside any volume.
-__device__ __forceinline__ void xform_coord(const XformSplit& X, int a, int x, int y, int z,
+__device__ __forceinline__ void xform_coord(const Xform& X, int a, int x, int y, int z,
                                             int& ib, float& fb) {
   const float fx = (float)x, fy = (float)y, fz = (float)z;  // exact: |x| < 2^24
   const float h0 = X.ah[3 * a], h1 = X.ah[3 * a + 1], h2 = X.ah[3 * a + 2];
@@ -176,9 +178,9 @@ struct TileBase {
 
 __device__ __forceinline__ void tile_base(const Xform* X, int x0, int y0, int z, TileBase& T) {
 #pragma unroll
-  for (int a = 0; a < 3; ++a) xform_coord(X->s, a, x0, y0, z, T.ib[a], T.fb[a]);
+  for (int a = 0; a < 3; ++a) xform_coord(*X, a, x0, y0, z, T.ib[a], T.fb[a]);
 #pragma unroll
-  for (int i = 0; i < 9; ++i) T.A[i] = X->s.ah[i];
+  for (int i = 0; i < 9; ++i) T.A[i] = X->ah[i];
 }
 
 // Trilinear (ND = 3) / bilinear (ND = 2) sample at offset (tx, ty) from the

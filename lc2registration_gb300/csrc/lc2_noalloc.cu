@@ -164,6 +164,7 @@ extern "C" int lc2_evaluate_noalloc(int mode, const lc2_geometry* virt, const lc
   // transform: moving-pixel coordinates of the virtual voxels
   lc2::Xform xf{};
   {
+    lc2::XformD D{};
     double L[3][3] = {{0}}, t[3] = {0};
     for (int a = 0; a < warp_nd; ++a) {
       for (int b = 0; b < warp_nd; ++b) L[a][b] = matrix[(warp_nd + 1) * a + b];
@@ -172,12 +173,12 @@ extern "C" int lc2_evaluate_noalloc(int mode, const lc2_geometry* virt, const lc
     for (int a = 0; a < 3; ++a) {
       double bs = t[a] - (double)moving->origin[a];
       for (int b = 0; b < 3; ++b) {
-        xf.A[3 * a + b] = L[a][b] * (double)virt->spacing[b] / (double)moving->spacing[a];
+        D.A[3 * a + b] = L[a][b] * (double)virt->spacing[b] / (double)moving->spacing[a];
         bs += L[a][b] * (double)virt->origin[b];
       }
-      xf.b[a] = (a < warp_nd) ? bs / (double)moving->spacing[a] : 0.0;
+      D.b[a] = (a < warp_nd) ? bs / (double)moving->spacing[a] : 0.0;
     }
-    lc2::xform_split(xf);
+    xf = lc2::xform_split(D);
   }
   NA_CUDA(cudaMemcpyAsync(&hdr->xf, &xf, sizeof(xf), cudaMemcpyHostToDevice, stream));
 
