@@ -236,14 +236,15 @@ __device__ __forceinline__ float fused_solve(const FusedParams& P, float sigma, 
   long long d_um = n * s_um - (long long)s_u * s_m;
   long long d_ug = n * s_ug - (long long)s_u * s_g;
   const bool km = d_mm > P.thr_m, kg = d_gg > P.thr_g;
-  const float iu = P.sig_scale / sigma;  // 1/sqrt(D_uu)
+  // fast divisions (2 ulp): sigma > 1e-3 and den in (1e-3, 1]
+  const float iu = __fdividef(P.sig_scale, sigma);  // 1/sqrt(D_uu)
   float r2 = 0.0f;
   if (km && kg) {
     float im = rsqrtf(ll2f(d_mm)), ig = rsqrtf(ll2f(d_gg));
     float rum = ll2f(d_um) * iu * im, rug = ll2f(d_ug) * iu * ig, rmg = ll2f(d_mg) * im * ig;
     float den = 1.0f - rmg * rmg;
     if (den > 1e-3f) {
-      r2 = (rum * rum + rug * rug - 2.0f * rum * rug * rmg) / den;
+      r2 = __fdividef(rum * rum + rug * rug - 2.0f * rum * rug * rmg, den);
     } else {
       // nearly collinear columns: solve in double from the exact sums
       double dmm = (double)d_mm, dgg = (double)d_gg, dmg = (double)d_mg;
@@ -279,6 +280,16 @@ __device__ __forceinline__ float fused_measure(const FusedParams& P, float sg, i
   return fused_solve(P, sg, s_u, L[0], L[1], Sx[0], Sx[1], Sx[2], Sx[3], Sx[4]);
 }
 
+// Square root of a Sobel magnitude: PTX sqrt.approx (one instruction, a
+// couple of ulp). The magnitude is quantised at 2^-19 of its range next, so
+// the approximation never moves a quantised value by more than one step and
+// LC2 by far less than 1e-7.
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // Sobel magnitude at plane index c (centre of a 3x3 in-plane neighbourhood).
 template <int ND, int PW>
 __device__ __forceinline__ float fused_sobel(const float* mc, const float* S, const float* D,
@@ -289,12 +300,12 @@ __device__ __forceinline__ float fused_sobel(const float* mc, const float* S, co
     float gy = (S[dn - 1] - S[up - 1]) + 2.0f * (S[dn] - S[up]) + (S[dn + 1] - S[up + 1]);
     float gz = (D[up - 1] + 2.0f * D[up] + D[up + 1]) + 2.0f * (D[c - 1] + 2.0f * D[c] + D[c + 1]) +
                (D[dn - 1] + 2.0f * D[dn] + D[dn + 1]);
-    return sqrtf(gx * gx + gy * gy + gz * gz);
+    return sqrt_approx(gx * gx + gy * gy + gz * gz);
   }
   const float* M = mc;
   float gx = (M[up + 1] - M[up - 1]) + 2.0f * (M[c + 1] - M[c - 1]) + (M[dn + 1] - M[dn - 1]);
   float gy = (M[dn - 1] - M[up - 1]) + 2.0f * (M[dn] - M[up]) + (M[dn + 1] - M[up + 1]);
-  return sqrtf(gx * gx + gy * gy);
+  return sqrt_approx(gx * gx + gy * gy);
 }
 
 // 3D Sobel magnitude at plane index c from the interleaved (Sz, Dz) plane:
@@ -310,7 +321,7 @@ __device__ __forceinline__ float fused_sobel_sd(const float2* SD, int c) {
   float gy = (c0.x - a0.x) + 2.0f * (c1.x - a1.x) + (c2.x - a2.x);
   float gz = (a0.y + 2.0f * a1.y + a2.y) + 2.0f * (b0.y + 2.0f * b1.y + b2.y) +
              (c0.y + 2.0f * c1.y + c2.y);
-  return sqrtf(gx * gx + gy * gy + gz * gz);
+  return sqrt_approx(gx * gx + gy * gy + gz * gz);
 }
 
 // Per-tile transform state in shared memory.
