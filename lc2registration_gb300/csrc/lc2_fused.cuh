@@ -675,24 +675,24 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
           lv_in[p] = qm;
           lv_in[G::NP + p] = qg;
           if constexpr (G::RINGW == 3) lv_in[2 * G::NP + p] = qu;
-          long long pin5[5] = {(long long)qu * qm, (long long)qu * qg, (long long)qm * qm,
-                               (long long)qg * qg, (long long)qm * qg};
-          int dqm = qm, dqg = qg;
+          accp[j][0] += (long long)qu * qm;
+          accp[j][1] += (long long)qu * qg;
+          accp[j][2] += (long long)qm * qm;
+          accp[j][3] += (long long)qg * qg;
+          accp[j][4] += (long long)qm * qg;
+          accq[j][0] += qm;
+          accq[j][1] += qg;
           if (leave) {
             const int qul = (G::RINGW == 3) ? lv_out[2 * G::NP + p] : quant(u_out[j], P.qu);
             const int qml = lv_out[p], qgl = lv_out[G::NP + p];
-            pin5[0] -= (long long)qul * qml;
-            pin5[1] -= (long long)qul * qgl;
-            pin5[2] -= (long long)qml * qml;
-            pin5[3] -= (long long)qgl * qgl;
-            pin5[4] -= (long long)qml * qgl;
-            dqm -= qml;
-            dqg -= qgl;
+            accp[j][0] -= (long long)qul * qml;
+            accp[j][1] -= (long long)qul * qgl;
+            accp[j][2] -= (long long)qml * qml;
+            accp[j][3] -= (long long)qgl * qgl;
+            accp[j][4] -= (long long)qml * qgl;
+            accq[j][0] -= qml;
+            accq[j][1] -= qgl;
           }
-          accq[j][0] += dqm;
-          accq[j][1] += dqg;
-#pragma unroll
-          for (int k = 0; k < 5; ++k) accp[j][k] += pin5[k];
           if (out) {
             // the same limb layout as fused_limbs: qM, qG, then (lo, hi) per product
             int* a = A + pa_off[j];
