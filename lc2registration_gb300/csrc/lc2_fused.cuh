@@ -192,16 +192,26 @@ __device__ __forceinline__ void fused_xy(int* __restrict__ A) {
       v[4 * i + 2] = q.z;
       v[4 * i + 3] = q.w;
     }
-    int a = 0;
+    // two independent sliding sums (outputs 0-15 and 16-31) for ILP
+    int a = 0, b = 0;
 #pragma unroll
-    for (int i = 0; i < G::W; ++i) a += v[i];
-    int o[4];
+    for (int i = 0; i < G::W; ++i) {
+      a += v[i];
+      b += v[16 + i];
+    }
+    int o[4], q[4];
     o[0] = a;
+    q[0] = b;
 #pragma unroll
-    for (int x = 1; x < 32; ++x) {
+    for (int x = 1; x < 16; ++x) {
       a += v[x + G::W - 1] - v[x - 1];
+      b += v[16 + x + G::W - 1] - v[16 + x - 1];
       o[x & 3] = a;
-      if ((x & 3) == 3) reinterpret_cast<int4*>(row)[x >> 2] = make_int4(o[0], o[1], o[2], o[3]);
+      q[x & 3] = b;
+      if ((x & 3) == 3) {
+        reinterpret_cast<int4*>(row)[x >> 2] = make_int4(o[0], o[1], o[2], o[3]);
+        reinterpret_cast<int4*>(row)[4 + (x >> 2)] = make_int4(q[0], q[1], q[2], q[3]);
+      }
     }
   }
   group_sync<BAR, G::NT>();
@@ -211,14 +221,21 @@ __device__ __forceinline__ void fused_xy(int* __restrict__ A) {
     int v[G::HY];
 #pragma unroll
     for (int i = 0; i < G::HY; ++i) v[i] = c[i * G::HXP];
-    int a = 0;
+    constexpr int H = TY / 2;  // two independent sliding sums (rows 0..H-1, H..TY-1)
+    int a = 0, b = 0;
 #pragma unroll
-    for (int i = 0; i < G::W; ++i) a += v[i];
+    for (int i = 0; i < G::W; ++i) {
+      a += v[i];
+      b += v[H + i];
+    }
     c[0] = a;
+    c[H * G::HXP] = b;
 #pragma unroll
-    for (int y = 1; y < TY; ++y) {
+    for (int y = 1; y < H; ++y) {
       a += v[y + G::W - 1] - v[y - 1];
+      b += v[H + y + G::W - 1] - v[H + y - 1];
       c[y * G::HXP] = a;
+      c[(H + y) * G::HXP] = b;
     }
   }
   group_sync<BAR, G::NT>();
