@@ -533,6 +533,11 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
   L.nd = c->lc2_nd;
   L.wnd = c->warp_nd;
   L.tile_height = c->tile_rows > 0 ? c->tile_rows : 16;
+  // a slice's tiles index one grid dimension (<= 65535): 8-row tiles only
+  // where they fit (16-row tiles always do, checked when the context is made)
+  if (L.tile_height == 8 &&
+      (long long)((c->virt.dim[0] + 31) / 32) * ((c->virt.dim[1] + 7) / 8) > 65535)
+    L.tile_height = 16;
   L.zchunk = c->zchunk;
   L.pipeline = c->pipeline;
   L.err = c->d_err;
@@ -665,7 +670,11 @@ int plan_context(const lc2_config* cfg, lc2_context* c) {
     c->virt.spacing[a] = cfg->virtual_spacing[a];
     if (a < c->warp_nd) {
       float ext = (float)c->cfg.fixed.dim[a] * c->cfg.fixed.spacing[a];
-      c->virt.dim[a] = (int)std::ceil((double)(ext / cfg->virtual_spacing[a]));
+      const double d = std::ceil((double)(ext / cfg->virtual_spacing[a]));
+      if (!(d <= (double)(1 << 20)))
+        return fail(LC2_ERR_UNSUPPORTED,
+                    "virtual grid axis %d would have %.0f voxels (at most 2^20)", a, d);
+      c->virt.dim[a] = (int)d;
     } else {
       c->virt.dim[a] = 1;
       c->virt.spacing[a] = 1.0f;
@@ -685,6 +694,16 @@ int plan_context(const lc2_config* cfg, lc2_context* c) {
     return fail(LC2_ERR_INVALID_ARGUMENT,
                 "2D-to-3D needs a single virtual slice (fixed z extent <= virtual z spacing)");
   c->nv = (size_t)c->virt.dim[0] * c->virt.dim[1] * c->virt.dim[2];
+  // 32-bit in-slice indices in the kernels; a slice's 32 x 16 tiles index
+  // one grid dimension of the fused launch (at most 65535)
+  if ((size_t)c->virt.dim[0] * c->virt.dim[1] >= (size_t)1 << 31 ||
+      (size_t)((c->virt.dim[0] + 31) / 32) * ((c->virt.dim[1] + 15) / 16) > 65535)
+    return fail(LC2_ERR_UNSUPPORTED, "virtual slice of %d x %d voxels is too large (at most "
+                "65535 tiles of 32 x 16)", c->virt.dim[0], c->virt.dim[1]);
+  if (c->lc2_nd == 3 && r > 4 &&
+      (size_t)((c->virt.dim[0] + 31) / 32) * ((c->virt.dim[1] + 7) / 8) > 65535)
+    return fail(LC2_ERR_UNSUPPORTED, "3D patches of radius > 4 run 32 x 8 tiles: a virtual slice "
+                "of %d x %d voxels needs more than 65535", c->virt.dim[0], c->virt.dim[1]);
   c->nf = (size_t)c->cfg.fixed.dim[0] * c->cfg.fixed.dim[1] * c->cfg.fixed.dim[2];
   c->nm = (size_t)c->cfg.moving.dim[0] * c->cfg.moving.dim[1] * c->cfg.moving.dim[2];
   if (c->nm >= (size_t)1 << 31 || c->nf >= (size_t)1 << 31)

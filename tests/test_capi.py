@@ -55,6 +55,18 @@ def test_rejects_bad_config_without_gpu():
     assert lib.lc2_create(None, ctypes.byref(h)) == 1
 
 
+@pytest.mark.parametrize("spacing", [1e-6, 0.001])
+def test_rejects_oversized_virtual_grid_without_gpu(spacing):
+    """A resampled spacing that would make the virtual grid overflow the
+    kernels' 32-bit slice indices or the 65535-tile grid limit is refused on
+    the host (status 6), before any device allocation."""
+    g = Geometry((512, 512, 1), (1, 1, 1), (0, 0, 0))
+    with pytest.raises(capi.LC2Error) as e:
+        capi.Context("2D", g, g, (spacing, spacing), patch_size=3)
+    assert e.value.status == 6
+    assert "virtual" in str(e.value)
+
+
 def test_singular_inverse_rejected():
     with pytest.raises(capi.LC2Error) as e:
         capi.invert_affine_3d(np.zeros((4, 4), dtype=np.float32))
