@@ -160,6 +160,12 @@ enum { LC2_OPTION_PIPELINE = 4 };
  * see cudaDeviceGetStreamPriorityRange). The server gives small requests the
  * most urgent priority so their launches are scheduled ahead of large ones. */
 enum { LC2_OPTION_STREAM_PRIORITY = 5 };
+/* LC2_OPTION_GENERIC: 1 evaluates through the generic kernels (resampling,
+ * Sobel and patch moments as separate launches through global scratch)
+ * instead of the fused kernel of the context's modality; for cross-checks.
+ * The values agree to FP32 resampling rounding (the two paths place their
+ * sampling bases differently). */
+enum { LC2_OPTION_GENERIC = 7 };
 int lc2_set_option(lc2_context* ctx, int option, int value);
 
 /* CUDA-graph launches issued by lc2_evaluate_batch / lc2_evaluate. */
@@ -170,8 +176,8 @@ long long lc2_graph_launches(const lc2_context* ctx);
  * warp-specialised, LC2_OPTION_PIPELINE) and z-chunk length it supports,
  * keeps the fastest as the context's options and returns the tile height
  * and z chunk. Contexts
- * without a tunable kernel (2D windows, HighResolutionModality: Fixed)
- * return their current settings. The reference takes fixed block sizes as
+ * without a tunable kernel (2D windows, mutual information, the generic
+ * path) return their current settings. The reference takes fixed block sizes as
  * arguments (src/cu_LC2/cu_lc2_3d.cuh:36-41). */
 int lc2_autotune(lc2_context* ctx, const float* matrices, int count, int* tile_rows, int* zchunk);
 

@@ -16,6 +16,7 @@
 #include "../../include/lc2.h"
 #include "lc2_kernels.cuh"
 #include "lc2_fused.cuh"
+#include "lc2_fused_fixed.cuh"
 #include "lc2_list.cuh"
 #include "lc2_mi.cuh"
 
@@ -154,6 +155,13 @@ struct lc2_context {
   float* d_sigma = nullptr;
   int* d_su = nullptr;  // window sum of the quantised static ultrasound per voxel
   long long sigma_sum = -1;
+  // resampled ultrasound (HighResolutionModality: Fixed): the static image
+  // and its Sobel quantised, their window sums and centred sums
+  // (lc2_fused_fixed.cuh)
+  int* d_fq = nullptr;
+  int* d_fs = nullptr;
+  long long* d_fd = nullptr;
+  int generic = 0;  // LC2_OPTION_GENERIC
   // normalised mutual information (patch_size 0): static image bins and
   // entropy, per-transform range and joint histogram
   bool mi = false;
@@ -195,7 +203,8 @@ struct lc2_context {
 namespace lc2 {
 // Exact window sum of width 2r+1 along one axis (0 = x, 1 = y, 2 = z) with
 // zero padding; one thread per line of the (nx, ny, nz) grid.
-__global__ void k_box_line(const int* __restrict__ in, int* __restrict__ out, int nx, int ny,
+template <typename T>
+__global__ void k_box_line(const T* __restrict__ in, T* __restrict__ out, int nx, int ny,
                            int nz, int axis, int r) {
   const long long line = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   size_t base, stride;
@@ -210,13 +219,41 @@ __global__ void k_box_line(const int* __restrict__ in, int* __restrict__ out, in
     if (line >= (long long)nx * ny) return;
     base = (size_t)line; stride = (size_t)nx * ny; len = nz;
   }
-  int a = 0;
+  T a = 0;
   for (int i = 0; i <= r && i < len; ++i) a += in[base + i * stride];
   out[base] = a;
   for (int i = 1; i < len; ++i) {
     if (i + r < len) a += in[base + (size_t)(i + r) * stride];
     if (i - r - 1 >= 0) a -= in[base + (size_t)(i - r - 1) * stride];
     out[base + (size_t)i * stride] = a;
+  }
+}
+
+// Resampled ultrasound: the static image M and its Sobel G quantised per
+// virtual voxel (q[2][nv]) and their products MM, GG, MG (p[3][nv]), the
+// fields whose window sums the fused kernel reads.
+__global__ void k_fixed_quant(const float* __restrict__ M, const float* __restrict__ G, size_t nv,
+                              float qm, float qg, int* __restrict__ q, long long* __restrict__ p) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int m = quant(M[i], qm), g = quant(G[i], qg);
+    q[i] = m;
+    q[nv + i] = g;
+    p[i] = (long long)m * m;
+    p[nv + i] = (long long)g * g;
+    p[2 * nv + i] = (long long)m * g;
+  }
+}
+
+// Window sums S_MM, S_GG, S_MG (d[3][nv]) -> centred sums n S_xy - S_x S_y.
+__global__ void k_fixed_centre(const int* __restrict__ s, long long* __restrict__ d, size_t nv,
+                               long long n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const long long sm = s[i], sg = s[nv + i];
+    d[i] = n * d[i] - sm * sm;
+    d[nv + i] = n * d[nv + i] - sg * sg;
+    d[2 * nv + i] = n * d[2 * nv + i] - sm * sg;
   }
 }
 
@@ -559,6 +596,35 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
 
 // Normalised mutual information of staged transforms [0, cnt): range,
 // joint histogram, entropies; results straight into d_out.
+// The fused kernel of a resampled ultrasound: one launch for `cnt` transforms.
+int launch_fused_fixed(lc2_context* c, int k0, int cnt) {
+  lc2::FixedLaunch L;
+  L.mov = c->d_moving;
+  L.S = lc2::FixedStatic{c->d_fq, c->d_fs, c->d_fd, c->nv};
+  L.P = c->fp;
+  L.xf = c->d_xf;
+  L.k0 = k0;
+  L.cnt = cnt;
+  L.acc = c->d_acc;
+  L.nd = c->lc2_nd;
+  L.wnd = c->warp_nd;
+  L.tile_height = c->tile_rows > 0 ? c->tile_rows : 16;
+  if (L.tile_height == 8 &&
+      (long long)((c->virt.dim[0] + 31) / 32) * ((c->virt.dim[1] + 7) / 8) > 65535)
+    L.tile_height = 16;
+  L.zchunk = c->zchunk;
+  L.stream = c->stream;
+  cudaError_t e;
+  switch (c->cfg.storage) {
+    case LC2_STORE_F16: e = lc2::fixed_launch<__half>(L); break;
+    case LC2_STORE_BF16: e = lc2::fixed_launch<__nv_bfloat16>(L); break;
+    default: e = lc2::fixed_launch<float>(L); break;
+  }
+  ++c->launches;
+  if (e != cudaSuccess) return fail(LC2_ERR_CUDA, "fused kernel (resampled ultrasound): %s", cudaGetErrorString(e));
+  return LC2_OK;
+}
+
 int launch_mi(lc2_context* c, int cnt) {
   const lc2_geometry& v = c->virt;
   lc2::MiParams P;
@@ -602,8 +668,9 @@ int launch_mi(lc2_context* c, int cnt) {
 
 // Enqueue the evaluation of staged transforms [k0, k0 + cnt).
 int launch_group(lc2_context* c, int k0, int cnt) {
+  if (c->generic) return launch_group_generic(c, k0, cnt, nullptr, nullptr);
   if (c->cfg.high_res_is_moving) return launch_fused(c, k0, cnt, nullptr);
-  return launch_group_generic(c, k0, cnt, nullptr, nullptr);
+  return launch_fused_fixed(c, k0, cnt);
 }
 
 int launch_finalize(lc2_context* c, int count) {
@@ -739,10 +806,13 @@ void context_bytes(const lc2_context* c, size_t* held, size_t* peak_extra) {
   h += c->nv * (hrm ? es : sizeof(float));     // static image on the virtual grid
   if (!hrm) h += c->nv * sizeof(float);        // its Sobel
   if (hrm && !c->mi) h += c->nv * (sizeof(float) + sizeof(int));  // weighting factors, S_U
+  if (!hrm && !c->mi) h += c->nv * (4 * sizeof(int) + 3 * sizeof(long long));  // static sums
   if (c->mi) h += c->nv + 64 * (sizeof(unsigned) * (lc2::kMiHist + 2));
   h += 64 * (sizeof(lc2::Xform) + 2 * sizeof(unsigned long long) + sizeof(double));
   *held = h;
   *peak_extra = std::max(c->nm, c->nf) * sizeof(float);
+  if (!hrm && !c->mi)  // temporaries of the static sums
+    *peak_extra = std::max(*peak_extra, c->nv * (sizeof(int) + sizeof(long long)));
 }
 
 int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
@@ -775,6 +845,12 @@ int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
   if (e == cudaSuccess && cfg->high_res_is_moving && !c->mi)
     e = dev_alloc((void**)&c->d_su, c->nv * sizeof(int), c->stream);
   if (e == cudaSuccess && c->mi) e = dev_alloc((void**)&c->d_sbin, c->nv, c->stream);
+  if (e == cudaSuccess && !cfg->high_res_is_moving && !c->mi)
+    e = dev_alloc((void**)&c->d_fq, 2 * c->nv * sizeof(int), c->stream);
+  if (e == cudaSuccess && !cfg->high_res_is_moving && !c->mi)
+    e = dev_alloc((void**)&c->d_fs, 2 * c->nv * sizeof(int), c->stream);
+  if (e == cudaSuccess && !cfg->high_res_is_moving && !c->mi)
+    e = dev_alloc((void**)&c->d_fd, 3 * c->nv * sizeof(long long), c->stream);
   if (e == cudaSuccess) e = dev_alloc((void**)&c->d_err, sizeof(int), c->stream);
   if (e == cudaSuccess) e = host_alloc((void**)&c->h_err, sizeof(int));
   if (e == cudaSuccess) e = cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
@@ -827,6 +903,9 @@ int lc2_destroy(lc2_context* c) {
   dev_free(c->d_gstatic, fs);
   dev_free(c->d_sigma, fs);
   dev_free(c->d_su, fs);
+  dev_free(c->d_fq, fs);
+  dev_free(c->d_fs, fs);
+  dev_free(c->d_fd, fs);
   dev_free(c->d_err, fs);
   dev_free(c->d_scratch, fs);
   dev_free(c->d_sbin, fs);
@@ -879,6 +958,14 @@ int lc2_set_option(lc2_context* c, int option, int value) {
     if (value == 16 && c->lc2_nd == 3 && c->cfg.patch_size > 4)
       return fail(LC2_ERR_UNSUPPORTED, "16-row tiles need a 3D patch radius <= 4");
     c->tile_rows = value;
+    drop_graphs(c);
+    return LC2_OK;
+  }
+  if (option == LC2_OPTION_GENERIC) {
+    if (value != 0 && value != 1) return fail(LC2_ERR_INVALID_ARGUMENT, "generic must be 0 or 1");
+    if (value == 1 && c->mi)
+      return fail(LC2_ERR_UNSUPPORTED, "mutual information has no generic LC2 path");
+    c->generic = value;
     drop_graphs(c);
     return LC2_OK;
   }
@@ -996,7 +1083,7 @@ int static_window_sum(lc2_context* c) {
     lc2::k_quant_static<float><<<blocks, 256, 0, c->stream>>>((const float*)c->d_static, nv, c->fp.qu, ta);
   const int nx = v.dim[0], ny = v.dim[1], nz = v.dim[2], r = c->cfg.patch_size;
   auto pass = [&](const int* in, int* out, int axis, long long lines) {
-    lc2::k_box_line<<<(unsigned)((lines + 127) / 128), 128, 0, c->stream>>>(in, out, nx, ny, nz,
+    lc2::k_box_line<int><<<(unsigned)((lines + 127) / 128), 128, 0, c->stream>>>(in, out, nx, ny, nz,
                                                                             axis, r);
   };
   pass(ta, tb, 0, (long long)ny * nz);
@@ -1007,6 +1094,62 @@ int static_window_sum(lc2_context* c) {
     pass(tb, c->d_su, 1, (long long)nx * nz);
   }
   c->launches += (c->lc2_nd == 3) ? 4 : 3;
+  LC2_CUDA(cudaGetLastError());
+  LC2_CUDA(cudaStreamSynchronize(c->stream));
+  return LC2_OK;
+}
+
+// Resampled ultrasound: quantised static image and Sobel, their exact window
+// sums and centred sums, once per context (the fields k_fused_fixed* read).
+int fixed_static_sums(lc2_context* c) {
+  const lc2_geometry& v = c->virt;
+  const size_t nv = c->nv;
+  const int nx = v.dim[0], ny = v.dim[1], nz = v.dim[2], r = c->cfg.patch_size;
+  int* ti = nullptr;
+  long long* tl = nullptr;
+  LC2_CUDA(dev_alloc((void**)&ti, nv * sizeof(int), c->stream));
+  struct Free {
+    void* p;
+    cudaStream_t st;
+    ~Free() { dev_free(p, st); }
+  } g1{ti, c->stream};
+  LC2_CUDA(dev_alloc((void**)&tl, nv * sizeof(long long), c->stream));
+  Free g2{tl, c->stream};
+  const int blocks = (int)std::min<size_t>((nv + 255) / 256, 152 * 16);
+  lc2::k_fixed_quant<<<blocks, 256, 0, c->stream>>>((const float*)c->d_static, c->d_gstatic, nv,
+                                                    c->fp.qm, c->fp.qg, c->d_fq, c->d_fd);
+  auto pass = [&](auto* in, auto* out, int axis) {
+    const long long lines = axis == 0 ? (long long)ny * nz : axis == 1 ? (long long)nx * nz
+                                                                       : (long long)nx * ny;
+    lc2::k_box_line<<<(unsigned)((lines + 127) / 128), 128, 0, c->stream>>>(in, out, nx, ny, nz,
+                                                                            axis, r);
+    ++c->launches;
+  };
+  // S_M, S_G: q -> s through x, y (, z) passes
+  for (int f = 0; f < 2; ++f) {
+    int* q = c->d_fq + f * nv;
+    int* o = c->d_fs + f * nv;
+    if (c->lc2_nd == 3) {
+      pass(q, o, 0);
+      pass(o, ti, 1);
+      pass(ti, o, 2);
+    } else {
+      pass(q, ti, 0);
+      pass(ti, o, 1);
+    }
+  }
+  // S_MM, S_GG, S_MG in place in d
+  for (int f = 0; f < 3; ++f) {
+    long long* p = c->d_fd + f * nv;
+    pass(p, tl, 0);
+    pass(tl, p, 1);
+    if (c->lc2_nd == 3) {
+      pass(p, tl, 2);
+      LC2_CUDA(cudaMemcpyAsync(p, tl, nv * sizeof(long long), cudaMemcpyDeviceToDevice, c->stream));
+    }
+  }
+  lc2::k_fixed_centre<<<blocks, 256, 0, c->stream>>>(c->d_fs, c->d_fd, nv, (long long)c->n);
+  c->launches += 2;
   LC2_CUDA(cudaGetLastError());
   LC2_CUDA(cudaStreamSynchronize(c->stream));
   return LC2_OK;
@@ -1122,6 +1265,7 @@ int set_fixed(lc2_context* c, const float* fixed, float fmax, float mmax) {
   F.qg = P.qg;
   F.thr_m = P.thr_m;
   F.thr_g = P.thr_g;
+  F.thr_var = P.thr_var;
   F.sig_scale = P.sig_scale;
   F.sum_scale = P.sum_scale;
   // limb split: every low limb's window sum (n+1 terms) stays below 2^30
@@ -1145,6 +1289,8 @@ int set_fixed(lc2_context* c, const float* fixed, float fmax, float mmax) {
     LC2_CUDA(cudaStreamSynchronize(c->stream));
     c->sigma_sum = (long long)sums[1];
     LC2_TRY(static_window_sum(c));
+  } else {
+    LC2_TRY(fixed_static_sums(c));
   }
   c->ready = true;
   return LC2_OK;
@@ -1932,7 +2078,8 @@ extern "C" int lc2_autotune(lc2_context* c, const float* matrices, int count, in
   if (count < 1) return fail(LC2_ERR_INVALID_ARGUMENT, "autotune needs at least one transform");
   LC2_TRY(select_device(c));
   const int r = c->cfg.patch_size;
-  if (c->lc2_nd == 3 && c->cfg.high_res_is_moving && !c->mi) {
+  const bool hrm = c->cfg.high_res_is_moving != 0;
+  if (c->lc2_nd == 3 && !c->mi && !c->generic) {
     LC2_TRY(lc2_stage_transforms(c, matrices, count));
     std::vector<int> rows = (r <= 4) ? std::vector<int>{16, 8} : std::vector<int>{8};
     const int vz = c->virt.dim[2];
@@ -1957,7 +2104,7 @@ extern "C" int lc2_autotune(lc2_context* c, const float* matrices, int count, in
     };
     std::vector<Cand> cands;
     for (int tr : rows) cands.push_back({tr, 0});
-    if (r <= 4) cands.push_back({16, 1});
+    if (r <= 4 && hrm) cands.push_back({16, 1});
     for (const Cand& cd : cands) {
       const int tr = cd.rows;
       for (int zc : chunks) {
@@ -1971,7 +2118,7 @@ extern "C" int lc2_autotune(lc2_context* c, const float* matrices, int count, in
             st = fail(LC2_ERR_CUDA, "autotune: %s", cudaGetErrorString(cudaGetLastError()));
             break;
           }
-          st = launch_fused(c, 0, count, nullptr);
+          st = hrm ? launch_fused(c, 0, count, nullptr) : launch_fused_fixed(c, 0, count);
           if (st == LC2_OK && (cudaEventRecord(b, c->stream) != cudaSuccess ||
                                cudaEventSynchronize(b) != cudaSuccess ||
                                cudaEventElapsedTime(&ms, a, b) != cudaSuccess))

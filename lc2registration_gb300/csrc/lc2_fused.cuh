@@ -40,6 +40,7 @@ struct FusedParams {
   int kbits;               // limb split K of the 64-bit products
   float qu, qm, qg;        // fixed-point scales
   long long thr_m, thr_g;  // degenerate-column thresholds (see MomentParams)
+  long long thr_var;       // valid-patch variance threshold (resampled ultrasound)
   float sig_scale;         // sigma = sqrt(D_uu) * sig_scale
   float sum_scale;         // fixed-point scale of the measure sum
 };
@@ -70,13 +71,6 @@ struct FusedGeom {
   static constexpr size_t OFF_A = OFF_LV + sizeof(int) * (size_t)RING * RINGW * NP;
   static constexpr size_t BYTES = OFF_A + sizeof(int) * (size_t)kLimbs * HY * HXP;
 };
-
-// int64 -> float through two 32-bit conversions (about 2 ulp).
-__device__ __forceinline__ float ll2f(long long v) {
-  const int hi = (int)(v >> 32);
-  const unsigned lo = (unsigned)(v & 0xffffffffll);
-  return fmaf((float)hi, 4294967296.0f, (float)lo);
-}
 
 // Trilinear / bilinear sample of the moving image at region point (px, py)
 // of the current slice; sb/sf: integer part and fraction of the region base.
@@ -160,11 +154,6 @@ __device__ __forceinline__ void fused_limbs(int qu, int qm, int qg, int K, int* 
   }
 }
 
-
-// x and y window passes in place on the limb planes A: after them, A rows
-// < TY, columns < 32 hold the patch sums. One thread per (limb, row), then
-// per (limb, column); each loads its whole row or column into registers
-// before writing, so the passes need no second buffer.
 // Barrier of the threads that run the window passes: the whole CTA (BAR = 0)
 // or, in the warp-specialised kernel, named barrier BAR of its NT threads.
 template <int BAR, int NT>
@@ -176,11 +165,14 @@ __device__ __forceinline__ void group_sync() {
   }
 }
 
-template <int ND, int TY, int R, int BAR = 0>
-__device__ __forceinline__ void fused_xy(int* __restrict__ A) {
+// x window pass in place over NL limb planes: afterwards rows < HY, columns
+// < 32 hold the x-window sums. One thread per (limb, row); each loads its row
+// into registers before writing.
+template <int ND, int TY, int R, int NL = kLimbs>
+__device__ __forceinline__ void fused_xpass(int* __restrict__ A) {
   using G = FusedGeom<ND, TY, R>;
   const int tid = threadIdx.x;
-  for (int it = tid; it < kLimbs * G::HY; it += G::NT) {
+  for (int it = tid; it < NL * G::HY; it += G::NT) {
     int* row = A + (size_t)it * G::HXP;  // it = limb * HY + row
     constexpr int NV = (G::HX + 3) / 4;   // 128-bit loads covering the row
     int v[4 * NV];
@@ -214,10 +206,21 @@ __device__ __forceinline__ void fused_xy(int* __restrict__ A) {
       }
     }
   }
-  group_sync<BAR, G::NT>();
-  for (int it = tid; it < kLimbs * 32; it += G::NT) {
+}
+
+// y window pass over the x-window sums: the patch sum of limb L at output
+// (column, row) goes to out[L * limb_stride + row * row_stride + column].
+// One thread per (limb, column); each loads its column first, so out may be
+// A itself.
+template <int ND, int TY, int R, int NL = kLimbs>
+__device__ __forceinline__ void fused_ypass(const int* A, int* out, int row_stride,
+                                            int limb_stride) {
+  using G = FusedGeom<ND, TY, R>;
+  const int tid = threadIdx.x;
+  for (int it = tid; it < NL * 32; it += G::NT) {
     const int L = it >> 5, col = it & 31;
-    int* c = A + (size_t)L * G::HY * G::HXP + col;
+    const int* c = A + (size_t)L * G::HY * G::HXP + col;
+    int* o = out + (size_t)L * limb_stride + col;
     int v[G::HY];
 #pragma unroll
     for (int i = 0; i < G::HY; ++i) v[i] = c[i * G::HXP];
@@ -228,16 +231,26 @@ __device__ __forceinline__ void fused_xy(int* __restrict__ A) {
       a += v[i];
       b += v[H + i];
     }
-    c[0] = a;
-    c[H * G::HXP] = b;
+    o[0] = a;
+    o[H * row_stride] = b;
 #pragma unroll
     for (int y = 1; y < H; ++y) {
       a += v[y + G::W - 1] - v[y - 1];
       b += v[H + y + G::W - 1] - v[H + y - 1];
-      c[y * G::HXP] = a;
-      c[(H + y) * G::HXP] = b;
+      o[y * row_stride] = a;
+      o[(H + y) * row_stride] = b;
     }
   }
+}
+
+// x and y window passes in place on the limb planes A: after them, A rows
+// < TY, columns < 32 hold the patch sums.
+template <int ND, int TY, int R, int BAR = 0, int NL = kLimbs>
+__device__ __forceinline__ void fused_xy(int* __restrict__ A) {
+  using G = FusedGeom<ND, TY, R>;
+  fused_xpass<ND, TY, R, NL>(A);
+  group_sync<BAR, G::NT>();
+  fused_ypass<ND, TY, R, NL>(A, A, G::HXP, G::HY * G::HXP);
   group_sync<BAR, G::NT>();
 }
 

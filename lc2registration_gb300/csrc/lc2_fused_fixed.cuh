@@ -1,0 +1,445 @@
+// lc2_fused_fixed.cuh -- fused LC2 evaluation for a resampled ultrasound
+// (HighResolutionModality: Fixed: the fixed MR/CT is the high-resolution
+// image, static on the virtual grid, and the moving ultrasound is resampled
+// for every transform; src/Interpolator/interpolator.cu:593-600,
+// :1346-1352).
+//
+// The static image M, its Sobel magnitude G and their patch sums do not change
+// with the transform, so the host precomputes them once per context
+// (k_fixed_quant, k_box_line, k_fixed_centre in lc2_capi.cu):
+//   q[2][nv]  M and G quantised per virtual voxel,
+//   s[2][nv]  their window sums S_M and S_G,
+//   d[3][nv]  the centred sums D_mm, D_gg, D_mg (D_xy = n S_xy - S_x S_y).
+// Per transform one CTA owns a 32 x TY output tile and, in 3D, marches along
+// z. Per entering slice it samples the ultrasound at its own halo points only
+// (no Sobel of the warped image is needed), updates in registers the exact
+// z-window sums of U, of the invalid-value count (a patch value <= 1e-6
+// invalidates the patch, src/cu_LC2/cu_lc2_3d.cu:223-243) and of the
+// products UU, UM, UG, and writes them as 8 int32 limbs; the x and y window
+// passes give the patch sums, and each output voxel's weighting factor and
+// measure come from solve_centred -- the generic kernel's solve. The
+// weighting factor depends on the transform here, so the kernel accumulates
+// both exact sums (measure and sigma) for k_finalize.
+#pragma once
+
+#include "lc2_fused.cuh"
+
+namespace lc2 {
+
+// Static precomputed fields of the high-resolution image, per virtual voxel.
+struct FixedStatic {
+  const int* q;        // quantised M, G: [2][nv]
+  const int* s;        // window sums S_M, S_G: [2][nv]
+  const long long* d;  // centred sums D_mm, D_gg, D_mg: [3][nv]
+  size_t nv;
+};
+
+// Limbs: S_U, invalid count, then (lo, hi) of UU, UM and UG.
+constexpr int kFixedLimbs = 8;
+
+// Shared memory of one CTA: the leaving ring (3D: 2R+2 slices of
+// (2 qU + invalid, qM, qG) per halo point), the limb planes, and in 3D the
+// patch sums of the previous output slice (solved while the next slice's
+// moments are formed).
+template <int ND, int TY, int R>
+struct FixedGeom {
+  using G = FusedGeom<ND, TY, R>;
+  static constexpr int RING = (ND == 3) ? 2 * R + 2 : 0;
+  static constexpr size_t OFF_A = sizeof(int) * (size_t)RING * 3 * G::NP;
+  static constexpr size_t OFF_Y = OFF_A + sizeof(int) * (size_t)kFixedLimbs * G::HY * G::HXP;
+  static constexpr size_t BYTES =
+      OFF_Y + ((ND == 3) ? sizeof(int) * (size_t)kFixedLimbs * TY * 32 : 0);
+};
+
+__device__ __forceinline__ void fixed_limbs(int* a, size_t pa, int su, int si, long long uu,
+                                            long long um, long long ug, int K) {
+  const unsigned long long mask = (1ull << K) - 1ull;
+  a[0] = su;
+  a[pa] = si;
+  a[2 * pa] = (int)((unsigned long long)uu & mask);
+  a[3 * pa] = (int)(uu >> K);
+  a[4 * pa] = (int)((unsigned long long)um & mask);
+  a[5 * pa] = (int)(um >> K);
+  a[6 * pa] = (int)((unsigned long long)ug & mask);
+  a[7 * pa] = (int)(ug >> K);
+}
+
+// Sigma and measure of output voxel gi from its patch sums (limb stride ls)
+// and the static fields; adds both to the exact sums.
+__device__ __forceinline__ void fixed_solve(const FusedParams& P, const FixedStatic& S,
+                                            const int* a, int ls, size_t gi, long long& acc_m,
+                                            long long& acc_s) {
+  if (a[ls] != 0) return;  // a patch value <= 1e-6: sigma = 0
+  const int su = a[0];
+  const long long uu = (long long)a[3 * ls] * (1LL << P.kbits) + a[2 * ls];
+  const long long um = (long long)a[5 * ls] * (1LL << P.kbits) + a[4 * ls];
+  const long long ug = (long long)a[7 * ls] * (1LL << P.kbits) + a[6 * ls];
+  const int sm = __ldg(S.s + gi), sg = __ldg(S.s + S.nv + gi);
+  const long long dmm = __ldg(S.d + gi), dgg = __ldg(S.d + S.nv + gi),
+                  dmg = __ldg(S.d + 2 * S.nv + gi);
+  const long long n = P.n;
+  float sigma, m;
+  solve_centred(n * uu - (long long)su * su, dmm, dgg, dmg, n * um - (long long)su * sm,
+                n * ug - (long long)su * sg, P.thr_var, P.thr_m, P.thr_g, P.sig_scale, sigma, m);
+  acc_m += __float2int_rn(m * P.sum_scale);
+  acc_s += __float2int_rn(sigma * P.sum_scale);
+}
+
+__device__ __forceinline__ void fixed_flush(long long acc_m, long long acc_s,
+                                            unsigned long long* acc) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    acc_m += __shfl_down_sync(0xffffffffu, acc_m, o);
+    acc_s += __shfl_down_sync(0xffffffffu, acc_s, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (acc_m) atomicAdd(acc, (unsigned long long)acc_m);
+    if (acc_s) atomicAdd(acc + 1, (unsigned long long)acc_s);
+  }
+}
+
+// ---- 3D: z-marching over output slices [zb, ze) ----
+template <typename TM, int TY, int R>
+__global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
+    k_fused_fixed3(const TM* __restrict__ mov, FixedStatic S, FusedParams P,
+                   const Xform* __restrict__ xf, int k0, unsigned long long* __restrict__ acc) {
+  using G = FusedGeom<3, TY, R>;
+  using F = FixedGeom<3, TY, R>;
+  constexpr int NT = G::NT, MAXP = G::MAXP, NL = kFixedLimbs;
+  constexpr size_t PA = (size_t)G::HY * G::HXP;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int* ring = reinterpret_cast<int*>(smem_raw);
+  int* A = reinterpret_cast<int*>(smem_raw + F::OFF_A);
+  int* Y = reinterpret_cast<int*>(smem_raw + F::OFF_Y);
+  __shared__ Xform s_xf;
+  __shared__ int s_ib[3];
+  __shared__ float s_fb[3];
+  __shared__ float s_A[9];
+  __shared__ int s_inside;
+  const int tid = threadIdx.x;
+  const int slot = blockIdx.x;
+  const int tile = blockIdx.y;
+  const int x0 = (tile % P.ntx) * 32, y0 = (tile / P.ntx) * TY;
+  const Xform* X = xf + k0 + slot;
+  // sampling base (x0 - R - 1, 16 floor(y0 / 16) - R - 1), as in k_fused, so
+  // 8- and 16-row tiles sample every voxel identically
+  const int gx0 = x0 - R - 1, gy0 = y0 - R - 1;
+  const int yb = y0 & 15;
+  const int ox = tid & 31, oy = tid >> 5;
+  const int zb = blockIdx.z * P.zchunk;
+  const int ze = min(zb + P.zchunk, P.vz);
+  const int e0 = zb - R;  // first slice entering the window
+  const size_t slice = (size_t)P.vx * P.vy;
+
+  auto set_base = [&](int zs) {
+    if (tid == NT - 1) {
+      bool in = zs >= 0 && zs < P.vz && gx0 >= 0 && gx0 + G::PW <= P.vx && gy0 >= 0 &&
+                gy0 + G::PH <= P.vy;
+      const int dims[3] = {P.mx, P.my, P.mz};
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        xform_coord(s_xf, a, gx0, gy0 - yb, zs, s_ib[a], s_fb[a]);
+        const float ex = s_A[3 * a] * (float)(G::PW - 1);
+        const float ea = s_A[3 * a + 1] * (float)yb, eb = s_A[3 * a + 1] * (float)(yb + G::PH - 1);
+        const float lo = s_fb[a] + fminf(ex, 0.0f) + fminf(ea, eb);
+        const float hi = s_fb[a] + fmaxf(ex, 0.0f) + fmaxf(ea, eb);
+        in = in && ((float)s_ib[a] + lo >= 0.01f) &&
+             ((float)s_ib[a] + hi <= (float)(dims[a] - 1) - 0.01f);
+      }
+      s_inside = in ? 1 : 0;
+    }
+  };
+  if (tid == 0) {
+    s_xf = *X;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) s_A[i] = X->ah[i];
+  }
+
+  // this thread's halo points: in-grid flag, in-slice index, A offset and
+  // region coordinates of the sampler
+  int pu[MAXP], pa_off[MAXP], ppx[MAXP], ppy[MAXP];
+  bool pin[MAXP];
+  int sU[MAXP], sI[MAXP];
+  long long sUU[MAXP], sUM[MAXP], sUG[MAXP];
+#pragma unroll
+  for (int j = 0; j < MAXP; ++j) {
+    const int p = tid + j * NT;
+    const int hy = p / G::HX, hx = p - hy * G::HX;
+    const int gx = x0 - R + hx, gy = y0 - R + hy;
+    pin[j] = (p < G::NP) && gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy;
+    pu[j] = pin[j] ? gy * P.vx + gx : 0;
+    pa_off[j] = hy * G::HXP + hx;
+    ppx[j] = hx + 1;
+    ppy[j] = hy + 1 + yb;
+    sU[j] = sI[j] = 0;
+    sUU[j] = sUM[j] = sUG[j] = 0;
+  }
+  long long acc_m = 0, acc_s = 0;
+  auto solve_out = [&](int z) {
+    const int x = x0 + ox, y = y0 + oy;
+    if (x < P.vx && y < P.vy)
+      fixed_solve(P, S, Y + oy * 32 + ox, TY * 32, ((size_t)z * P.vy + y) * P.vx + x, acc_m,
+                  acc_s);
+  };
+
+  __syncthreads();  // s_xf, s_A
+  set_base(e0);
+  __syncthreads();
+  // Three phases per entering slice e, one barrier after each:
+  //   1: solve output slice z-1 from Y; sample slice e, update the z-window
+  //      sums and write the limbs;
+  //   2: x window pass; sampling base of slice e+1;
+  //   3: y window pass into Y.
+  bool pending = false;  // Y holds the patch sums of output slice z-1
+  for (int e = e0; e < ze + R; ++e) {
+    const int z = e - R;          // output slice completed by this entering slice
+    const int l = e - 2 * R - 1;  // slice leaving the window
+    const bool out = (z >= zb);
+    const bool leave = (l >= e0);
+    const bool zin = (e >= 0 && e < P.vz);
+    if (pending) solve_out(z - 1);
+    int* rin = ring + ((e - e0) % F::RING) * 3 * G::NP;
+    const int* rout = ring + ((l - e0 + F::RING) % F::RING) * 3 * G::NP;
+    const bool inside = s_inside;
+#pragma unroll
+    for (int j = 0; j < MAXP; ++j) {
+      const int p = tid + j * NT;
+      if (p < G::NP) {
+        float u = 0.0f;
+        int qm = 0, qg = 0;
+        if (inside) {
+          u = fused_sample_inside<TM>(mov, P, s_A, s_ib, s_fb, ppx[j], ppy[j]);
+        } else if (pin[j] && zin) {
+          u = fused_sample<3, TM>(mov, P, s_A, s_ib, s_fb, ppx[j], ppy[j]);
+        }
+        if (pin[j] && zin) {
+          const size_t gi = (size_t)e * slice + pu[j];
+          qm = __ldg(S.q + gi);
+          qg = __ldg(S.q + S.nv + gi);
+        }
+        const int qu = quant(u, P.qu), inv = (u > 1e-6f) ? 0 : 1;
+        rin[p] = 2 * qu + inv;
+        rin[G::NP + p] = qm;
+        rin[2 * G::NP + p] = qg;
+        sU[j] += qu;
+        sI[j] += inv;
+        sUU[j] += (long long)qu * qu;
+        sUM[j] += (long long)qu * qm;
+        sUG[j] += (long long)qu * qg;
+        if (leave) {
+          const int pl = rout[p], qml = rout[G::NP + p], qgl = rout[2 * G::NP + p];
+          const int qul = pl >> 1;
+          sU[j] -= qul;
+          sI[j] -= pl & 1;
+          sUU[j] -= (long long)qul * qul;
+          sUM[j] -= (long long)qul * qml;
+          sUG[j] -= (long long)qul * qgl;
+        }
+        if (out) fixed_limbs(A + pa_off[j], PA, sU[j], sI[j], sUU[j], sUM[j], sUG[j], P.kbits);
+      }
+    }
+    __syncthreads();
+    if (out) fused_xpass<3, TY, R, NL>(A);
+    set_base(e + 1);
+    __syncthreads();
+    if (out) fused_ypass<3, TY, R, NL>(A, Y, 32, TY * 32);
+    pending = out;
+    __syncthreads();
+  }
+  if (pending) solve_out(ze - 1);
+  fixed_flush(acc_m, acc_s, acc + 2 * (size_t)(k0 + slot));
+}
+
+// ---- 2D and 2D-to-3D: one 32 x 16 tile per CTA ----
+// Three CTAs per SM (42 registers): the solve's 64-bit work spills at the
+// 32 registers of four.
+template <int WND, typename TM, int R>
+__global__ void __launch_bounds__(512, 3)
+    k_fused_fixed2(const TM* __restrict__ mov, FixedStatic S, FusedParams P,
+                   const Xform* __restrict__ xf, int k0, unsigned long long* __restrict__ acc) {
+  constexpr int TY = 16;
+  using G = FusedGeom<2, TY, R>;
+  constexpr int NT = G::NT, NL = kFixedLimbs;
+  constexpr size_t PA = (size_t)G::HY * G::HXP;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int* A = reinterpret_cast<int*>(smem_raw + FixedGeom<2, TY, R>::OFF_A);
+  __shared__ TileShared T;
+  const int tid = threadIdx.x;
+  const int slot = blockIdx.x;
+  const int tile = blockIdx.y;
+  const Xform* X = xf + k0 + slot;
+  const int x0 = (tile % P.ntx) * 32, y0 = (tile / P.ntx) * TY;
+  const int gx0 = x0 - R - 1, gy0 = y0 - R - 1;
+  if (tid == 0) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) xform_coord(*X, a, gx0, gy0, 0, T.ib[a], T.fb[a]);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) T.A[i] = X->ah[i];
+    bool in = gx0 >= 0 && gx0 + G::PW <= P.vx && gy0 >= 0 && gy0 + G::PH <= P.vy;
+    const int dims[3] = {P.mx, P.my, P.mz};
+#pragma unroll
+    for (int a = 0; a < WND; ++a) {
+      const float ex = T.A[3 * a] * (float)(G::PW - 1), ey = T.A[3 * a + 1] * (float)(G::PH - 1);
+      const float lo = T.fb[a] + fminf(ex, 0.0f) + fminf(ey, 0.0f);
+      const float hi = T.fb[a] + fmaxf(ex, 0.0f) + fmaxf(ey, 0.0f);
+      in = in && ((float)T.ib[a] + lo >= 0.01f) &&
+           ((float)T.ib[a] + hi <= (float)(dims[a] - 1) - 0.01f);
+    }
+    T.inside = in ? 1 : 0;
+  }
+  __syncthreads();
+  const bool inside = T.inside;
+  for (int p = tid; p < G::NP; p += NT) {
+    const int hy = p / G::HX, hx = p - hy * G::HX;
+    const int gx = x0 - R + hx, gy = y0 - R + hy;
+    const bool pin = gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy;
+    float u = 0.0f;
+    int qm = 0, qg = 0;
+    if (inside) {
+      if constexpr (WND == 3)
+        u = fused_sample_inside<TM>(mov, P, T.A, T.ib, T.fb, hx + 1, hy + 1);
+      else
+        u = fused_sample_inside2<TM>(mov, P, T.A, T.ib, T.fb, hx + 1, hy + 1);
+    } else if (pin) {
+      u = fused_sample<WND, TM>(mov, P, T.A, T.ib, T.fb, hx + 1, hy + 1);
+    }
+    if (pin) {
+      const size_t gi = (size_t)gy * P.vx + gx;
+      qm = __ldg(S.q + gi);
+      qg = __ldg(S.q + S.nv + gi);
+    }
+    const int qu = quant(u, P.qu);
+    fixed_limbs(A + hy * G::HXP + hx, PA, qu, (u > 1e-6f) ? 0 : 1, (long long)qu * qu,
+                (long long)qu * qm, (long long)qu * qg, P.kbits);
+  }
+  __syncthreads();
+  fused_xy<2, TY, R, 0, NL>(A);
+  long long acc_m = 0, acc_s = 0;
+  const int ox = tid & 31, oy = tid >> 5;
+  const int x = x0 + ox, y = y0 + oy;
+  if (x < P.vx && y < P.vy)
+    fixed_solve(P, S, A + oy * G::HXP + ox, (int)PA, (size_t)y * P.vx + x, acc_m, acc_s);
+  fixed_flush(acc_m, acc_s, acc + 2 * (size_t)(k0 + slot));
+}
+
+struct FixedLaunch {
+  const void* mov;
+  FixedStatic S;
+  FusedParams P;
+  const Xform* xf;
+  int k0, cnt;
+  unsigned long long* acc;
+  int nd, wnd;
+  int tile_height;  // 3D, radius <= 4: 16 or 8 rows per tile
+  int zchunk;       // 3D: output slices per CTA; 0 = automatic
+  cudaStream_t stream;
+};
+
+template <typename T, int R, int TY>
+cudaError_t fixed_launch3(const FixedLaunch& L) {
+  using F = FixedGeom<3, TY, R>;
+  auto kern = k_fused_fixed3<T, TY, R>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)F::BYTES);
+  if (e != cudaSuccess) return e;
+  FusedParams P = L.P;
+  const int ntx = (P.vx + 31) / 32, nty = (P.vy + TY - 1) / TY;
+  P.ntx = ntx;
+  int nz;
+  if (L.zchunk > 0) {
+    P.zchunk = L.zchunk < P.vz ? L.zchunk : P.vz;
+  } else {
+    const long long ctas = (long long)ntx * nty * L.cnt;
+    nz = (int)((4LL * 152 + ctas - 1) / ctas);
+    nz = nz < 1 ? 1 : nz;
+    int cap = P.vz / (4 * R + 4);
+    cap = cap < 1 ? 1 : cap;
+    nz = nz > cap ? cap : nz;
+    P.zchunk = (P.vz + nz - 1) / nz;
+  }
+  nz = (P.vz + P.zchunk - 1) / P.zchunk;
+  dim3 grid(L.cnt, ntx * nty, nz);
+  kern<<<grid, 32 * TY, F::BYTES, L.stream>>>((const T*)L.mov, L.S, P, L.xf, L.k0, L.acc);
+  return cudaGetLastError();
+}
+
+template <typename T, int R>
+cudaError_t fixed_launch2(const FixedLaunch& L) {
+  using F = FixedGeom<2, 16, R>;
+  FusedParams P = L.P;
+  P.ntx = (P.vx + 31) / 32;
+  const int nty = (P.vy + 15) / 16;
+  dim3 grid(L.cnt, P.ntx * nty, 1);
+  if (L.wnd == 3) {
+    auto kern = k_fused_fixed2<3, T, R>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)F::BYTES);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, 512, F::BYTES, L.stream>>>((const T*)L.mov, L.S, P, L.xf, L.k0, L.acc);
+  } else {
+    auto kern = k_fused_fixed2<2, T, R>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)F::BYTES);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, 512, F::BYTES, L.stream>>>((const T*)L.mov, L.S, P, L.xf, L.k0, L.acc);
+  }
+  return cudaGetLastError();
+}
+
+// Tile heights as for k_fused: 16 rows (or 8 on request) up to radius 4,
+// 8 rows beyond.
+template <typename T, int R>
+cudaError_t fixed_launch_r(const FixedLaunch& L) {
+  if (L.nd == 2) return fixed_launch2<T, R>(L);
+  if constexpr (R <= 6) {
+    if constexpr (R > 4) {
+      return fixed_launch3<T, R, 8>(L);
+    } else {
+      if (L.tile_height == 8) return fixed_launch3<T, R, 8>(L);
+      return fixed_launch3<T, R, 16>(L);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <typename T>
+cudaError_t fixed_launch_t(const FixedLaunch& L) {
+  switch (L.P.r) {
+    case 1: return fixed_launch_r<T, 1>(L);
+    case 2: return fixed_launch_r<T, 2>(L);
+    case 3: return fixed_launch_r<T, 3>(L);
+    case 4: return fixed_launch_r<T, 4>(L);
+    case 5: return fixed_launch_r<T, 5>(L);
+    case 6: return fixed_launch_r<T, 6>(L);
+  }
+  if (L.nd == 2) {
+    switch (L.P.r) {
+      case 7: return fixed_launch2<T, 7>(L);
+      case 8: return fixed_launch2<T, 8>(L);
+      case 9: return fixed_launch2<T, 9>(L);
+      case 10: return fixed_launch2<T, 10>(L);
+      case 11: return fixed_launch2<T, 11>(L);
+      case 12: return fixed_launch2<T, 12>(L);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+// Defined per storage type in lc2_fixed_{f32,f16,bf16}.cu.
+template <typename T>
+cudaError_t fixed_launch(const FixedLaunch& L);
+
+template <>
+cudaError_t fixed_launch<float>(const FixedLaunch& L);
+template <>
+cudaError_t fixed_launch<__half>(const FixedLaunch& L);
+template <>
+cudaError_t fixed_launch<__nv_bfloat16>(const FixedLaunch& L);
+
+#define LC2_DEFINE_FIXED_LAUNCH(T)                      \
+  template <>                                           \
+  cudaError_t fixed_launch<T>(const FixedLaunch& L) {   \
+    return fixed_launch_t<T>(L);                        \
+  }
+
+}  // namespace lc2

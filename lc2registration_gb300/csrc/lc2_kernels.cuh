@@ -322,6 +322,14 @@ struct MomentParams {
   size_t u_stride, m_stride, g_stride;  // per-slot strides (0 for static images)
 };
 
+// int64 -> float through two 32-bit conversions (about 2 ulp; the single
+// 64-bit conversion is a slow multi-cycle instruction).
+__device__ __forceinline__ float ll2f(long long v) {
+  const int hi = (int)(v >> 32);
+  const unsigned lo = (unsigned)(v & 0xffffffffll);
+  return fmaf((float)hi, 4294967296.0f, (float)lo);
+}
+
 // Round v*Q to the nearest integer (|v*Q| < 2^22): add 1.5*2^23 and read the
 // integer out of the mantissa.
 __device__ __forceinline__ int quant(float v, float Q) {
@@ -480,6 +488,53 @@ __device__ __forceinline__ void mom_xy_passes(const MomSmem& s, int r) {
   __syncthreads();
 }
 
+// Sigma and clipped measure from centred sums D_xy = n S_xy - S_x S_y of a
+// valid patch (every value > 1e-6). Shared by the generic moments kernel and
+// the fused kernel of a resampled ultrasound, so both give the same bits.
+__device__ __forceinline__ void solve_centred(long long d_uu, long long d_mm, long long d_gg,
+                                              long long d_mg, long long d_um, long long d_ug,
+                                              long long thr_var, long long thr_m,
+                                              long long thr_g, float sig_scale, float& sigma,
+                                              float& measure) {
+  sigma = 0.0f;
+  measure = 0.0f;
+  if (d_uu <= thr_var) return;
+  const float fuu = ll2f(d_uu);
+  sigma = sqrtf(fuu) * sig_scale;
+  const bool km = d_mm > thr_m, kg = d_gg > thr_g;
+  const float iu = rsqrtf(fuu);
+  float r2 = 0.0f;
+  if (km && kg) {
+    const float im = rsqrtf(ll2f(d_mm)), ig = rsqrtf(ll2f(d_gg));
+    const float rum = ll2f(d_um) * iu * im, rug = ll2f(d_ug) * iu * ig,
+                rmg = ll2f(d_mg) * im * ig;
+    const float den = 1.0f - rmg * rmg;
+    if (den > 1e-3f) {
+      r2 = __fdividef(rum * rum + rug * rug - 2.0f * rum * rug * rmg, den);
+    } else {
+      // nearly collinear columns: solve in double from the exact sums
+      double duu = (double)d_uu, dmm = (double)d_mm, dgg = (double)d_gg;
+      double dmg = (double)d_mg, dum = (double)d_um, dug = (double)d_ug;
+      double det = dmm * dgg - dmg * dmg;
+      double e;
+      if (det <= 1e-10 * dmm * dgg)
+        e = dum * dum / dmm;
+      else
+        e = (dgg * dum * dum - 2.0 * dmg * dum * dug + dmm * dug * dug) / det;
+      r2 = (float)(e / duu);
+    }
+  } else if (km) {
+    const float c = ll2f(d_um) * iu * rsqrtf(ll2f(d_mm));
+    r2 = c * c;
+  } else if (kg) {
+    const float c = ll2f(d_ug) * iu * rsqrtf(ll2f(d_gg));
+    r2 = c * c;
+  }
+  float m = sigma * r2;
+  if (!(m > 0.0f) || isinf(m)) m = 0.0f;
+  measure = m;
+}
+
 // Per-voxel sigma and clipped measure from exact patch sums.
 // Reference semantics: sigma = sqrt(sample variance of U) when every patch
 // value is > 1e-6 and the variance is > 1e-6, else 0; measure =
@@ -495,44 +550,10 @@ __device__ __forceinline__ void solve_voxel(const MomentParams& P, int s_u, int 
   measure = 0.0f;
   if (cnt != 0) return;
   const long long n = P.n;
-  long long d_uu = n * s_uu - (long long)s_u * s_u;
-  if (d_uu <= P.thr_var) return;
-  sigma = sqrtf((float)d_uu) * P.sig_scale;
-  long long d_mm = n * s_mm - (long long)s_m * s_m;
-  long long d_gg = n * s_gg - (long long)s_g * s_g;
-  long long d_mg = n * s_mg - (long long)s_m * s_g;
-  long long d_um = n * s_um - (long long)s_u * s_m;
-  long long d_ug = n * s_ug - (long long)s_u * s_g;
-  const bool km = d_mm > P.thr_m, kg = d_gg > P.thr_g;
-  float r2 = 0.0f;
-  if (km && kg) {
-    float iu = rsqrtf((float)d_uu), im = rsqrtf((float)d_mm), ig = rsqrtf((float)d_gg);
-    float rum = (float)d_um * iu * im, rug = (float)d_ug * iu * ig, rmg = (float)d_mg * im * ig;
-    float den = 1.0f - rmg * rmg;
-    if (den > 1e-3f) {
-      r2 = (rum * rum + rug * rug - 2.0f * rum * rug * rmg) / den;
-    } else {
-      // nearly collinear columns: solve in double from the exact sums
-      double duu = (double)d_uu, dmm = (double)d_mm, dgg = (double)d_gg;
-      double dmg = (double)d_mg, dum = (double)d_um, dug = (double)d_ug;
-      double det = dmm * dgg - dmg * dmg;
-      double e;
-      if (det <= 1e-10 * dmm * dgg)
-        e = dum * dum / dmm;
-      else
-        e = (dgg * dum * dum - 2.0 * dmg * dum * dug + dmm * dug * dug) / det;
-      r2 = (float)(e / duu);
-    }
-  } else if (km) {
-    float c = (float)d_um * rsqrtf((float)d_uu) * rsqrtf((float)d_mm);
-    r2 = c * c;
-  } else if (kg) {
-    float c = (float)d_ug * rsqrtf((float)d_uu) * rsqrtf((float)d_gg);
-    r2 = c * c;
-  }
-  float m = sigma * r2;
-  if (!(m > 0.0f) || isinf(m)) m = 0.0f;
-  measure = m;
+  solve_centred(n * s_uu - (long long)s_u * s_u, n * s_mm - (long long)s_m * s_m,
+                n * s_gg - (long long)s_g * s_g, n * s_mg - (long long)s_m * s_g,
+                n * s_um - (long long)s_u * s_m, n * s_ug - (long long)s_u * s_g, P.thr_var,
+                P.thr_m, P.thr_g, P.sig_scale, sigma, measure);
 }
 
 // Accumulate one voxel into the thread's exact sums.

@@ -1,0 +1,109 @@
+"""GPU parity of the fused kernel of a resampled ultrasound
+(HighResolutionModality: Fixed: the MR/CT is the static high-resolution
+image, the ultrasound is warped per transform) against the FP64 oracle and
+against the generic path (LC2_OPTION_GENERIC), through the C ABI.
+
+Tolerances: LC2 within 1e-5 relative of the oracle (the benchmark spec's bound);
+fused against generic within 1e-6 relative (the two place their sampling
+bases differently, so an interpolated value can differ in its last bit and a
+quantised ultrasound value by one step); tile heights, batch vs plain: bit-
+identical (exact integer sums).
+"""
+import numpy as np
+import pytest
+
+from lc2registration_gb300 import capi
+from tests.helpers import make_context, oracle_eval, perturbed
+from tests.test_gpu_parity import REL_LC2, _case, _hr_fixed
+
+pytestmark = pytest.mark.gpu
+
+KINDS = ["2d", "2d_r1", "2d_r9", "3d", "3d_r3", "3d_r4", "3d_r5", "3d_r6"]
+
+
+def _fixed(kind, n, seed=5, scale=0.5):
+    """The case with the roles of HighResolutionModality: Fixed and n
+    transforms around its true one (inverses of the moving-mode ones)."""
+    base = _case(kind)
+    mats = perturbed(base, np.random.default_rng(seed), n, scale=scale)
+    inv = np.linalg.inv(mats.astype(np.float64)).astype(np.float32)
+    case = _hr_fixed(base)
+    return case, np.concatenate([case.true_mat[None], inv])
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_fixed_fused_matches_oracle(kind):
+    case, mats = _fixed(kind, 2)
+    ctx = make_context(case)
+    got = ctx.evaluate_batch(mats)
+    for k in range(len(mats)):
+        ref = oracle_eval(case, mats[k], use_boxsum=False)
+        assert ref > 0.01
+        assert abs(got[k] / ref - 1.0) < REL_LC2, (k, got[k], ref)
+
+
+@pytest.mark.parametrize("kind", ["2d", "2d_r9", "3d", "3d_r4", "3d_r6"])
+def test_fixed_fused_matches_generic_path(kind):
+    case, mats = _fixed(kind, 5)
+    ctx = make_context(case)
+    fused = ctx.evaluate_batch(mats)
+    ctx.set_option(capi.OPTION_GENERIC, 1)
+    generic = ctx.evaluate_batch(mats)
+    ctx.set_option(capi.OPTION_GENERIC, 0)
+    np.testing.assert_allclose(fused, generic, rtol=1e-6, atol=0)
+    # the generic LC2 of evaluate_fields agrees too
+    lc2_fields, _ = ctx.evaluate_fields(mats[0])
+    assert abs(lc2_fields / fused[0] - 1.0) < 1e-6
+
+
+@pytest.mark.parametrize("kind", ["3d", "3d_r4"])
+def test_fixed_tile_heights_and_zchunks_bitwise(kind):
+    case, mats = _fixed(kind, 3)
+    ctx = make_context(case)
+    base = ctx.evaluate_batch(mats)
+    for rows, zc in [(8, 0), (16, 7), (8, 13)]:
+        ctx.set_option(capi.OPTION_TILE_ROWS, rows)
+        ctx.set_option(capi.OPTION_ZCHUNK, zc)
+        assert np.array_equal(ctx.evaluate_batch(mats), base), (rows, zc)
+    ctx.set_option(capi.OPTION_TILE_ROWS, 0)
+    ctx.set_option(capi.OPTION_ZCHUNK, 0)
+
+
+@pytest.mark.parametrize("kind", ["2d", "3d"])
+def test_fixed_batch_equals_plain_bitwise(kind):
+    case, mats = _fixed(kind, 6)
+    ctx = make_context(case, max_batch=3)
+    batch = ctx.evaluate_batch(mats)
+    plain = np.array([ctx.evaluate(m) for m in mats])
+    assert np.array_equal(batch, plain)
+
+
+@pytest.mark.parametrize("storage", ["f16", "bf16"])
+@pytest.mark.parametrize("kind", ["2d", "3d_r4"])
+def test_fixed_reduced_storage_matches_oracle_on_rounded_inputs(kind, storage):
+    case, mats = _fixed(kind, 2)
+    ctx = make_context(case, storage=storage)
+    got = ctx.evaluate_batch(mats)
+    for k in range(len(mats)):
+        ref = oracle_eval(case, mats[k], storage=storage)
+        assert abs(got[k] / ref - 1.0) < REL_LC2, (k, got[k], ref)
+
+
+def test_fixed_autotune_keeps_values():
+    case, mats = _fixed("3d_r3", 4)
+    ctx = make_context(case)
+    before = ctx.evaluate_batch(mats)
+    rows, zc = ctx.autotune(mats)
+    assert rows in (8, 16)
+    assert np.array_equal(ctx.evaluate_batch(mats), before)
+
+
+def test_fixed_degenerate_inputs():
+    """Out-of-view transform: the warped ultrasound is 0 everywhere, every
+    patch is invalid, LC2 = 0/0 -> 0 on the GPU as in the oracle."""
+    case, mats = _fixed("3d", 1)
+    away = mats[0].copy()
+    away[0, -1] += 1e4
+    ctx = make_context(case)
+    assert ctx.evaluate(away) == 0.0
+    assert oracle_eval(case, away) == 0.0
