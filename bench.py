@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="default launch options")
     ap.add_argument("--no-small", action="store_true", help="skip the 2D 256^2 / 3D 96^3 lines")
     ap.add_argument("--no-stack", action="store_true", help="skip the 2D-to-3D frame-stack line")
+    ap.add_argument("--no-fixed", action="store_true",
+                    help="skip the HighResolutionModality: Fixed lines")
     ap.add_argument("--stack-frames", type=int, default=64)
     ap.add_argument("--stack-poses", type=int, default=256)
     ap.add_argument("--serve-requests", type=int, default=48)
@@ -320,6 +322,72 @@ def small_configs(device):
     return out
 
 
+def fixed_leg(args, main_case, device):
+    """HighResolutionModality: Fixed (the reference's own configs use it): the
+    MR/CT is the static high-resolution image on its own grid and the
+    ultrasound is warped per transform. The same volumes with the roles
+    swapped: device-timed batches through the fused kernel of this modality,
+    the same batches through the generic kernels (LC2_OPTION_GENERIC), and one
+    lc2_evaluate per transform."""
+    import numpy as np
+    import torch
+
+    from lc2registration_gb300 import capi, synth
+    from tests.helpers import perturbed
+
+    def swapped(case):
+        return synth.Case(case.mode, case.moving_geom, case.moving, case.fixed_geom, case.fixed,
+                          list(case.moving_geom.spacing[: (2 if case.mode == "2D" else 3)]),
+                          case.r, hr_moving=False, true_params={},
+                          true_mat=np.linalg.inv(case.true_mat.astype(np.float64)).astype(np.float32))
+
+    def timed(ctx, K, reps):
+        stream = torch.cuda.ExternalStream(ctx.stream())
+        for _ in range(2):
+            ctx.launch(K)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for _ in range(reps):
+            ctx.launch(K)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        return reps * K / (ev[0].elapsed_time(ev[1]) / 1e3)
+
+    out = {}
+    for name, base, K, storage, plain_n in (
+            (f"3d_{args.size}_r{args.patch}", main_case, 128, args.storage, 24),
+            ("2d_256_r3", synth.case_2d(seed=7, size=256, r=3), 512, "f32", 200),
+            ("3d_128_96_r3", synth.case_3d(seed=8, mr_size=128, us_size=96, r=3), 256, "f32", 100)):
+        case = swapped(base)
+        mats = np.linalg.inv(perturbed(base, np.random.default_rng(3), K).astype(np.float64))
+        mats = mats.astype(np.float32)
+        ctx = capi.Context(case.mode, case.fixed_geom, case.moving_geom, case.virt_spacing, case.r,
+                           False, storage, device=device)
+        ctx.set_images(case.fixed, case.moving)
+        ctx.stage(mats)
+        fused = timed(ctx, K, 5)
+        vals = ctx.fetch(K)
+        ctx.set_option(capi.OPTION_GENERIC, 1)
+        generic = timed(ctx, K, 3)
+        gvals = ctx.fetch(K)
+        ctx.set_option(capi.OPTION_GENERIC, 0)
+        for m in mats[:4]:
+            ctx.evaluate(m)
+        t0 = time.perf_counter()
+        plain = [ctx.evaluate(m) for m in mats[:plain_n]]
+        plain_eps = len(plain) / (time.perf_counter() - t0)
+        assert np.array_equal(np.array(plain), vals[:len(plain)]), "plain != batched"
+        out[name] = {"batched_evals_per_s": fused, "generic_batched_evals_per_s": generic,
+                     "fused_over_generic": fused / generic, "plain_evals_per_s": plain_eps,
+                     "max_rel_diff_fused_generic": float(np.max(np.abs(vals - gvals) /
+                                                               np.maximum(np.abs(gvals), 1e-30))),
+                     "candidates_per_launch": K, "virtual_voxels": int(np.prod(ctx.virtual_dims())),
+                     "storage": storage}
+        ctx.close()
+    return out
+
+
 def stack_leg(args, main_case, device):
     """2D-to-3D frame stack: frames of uneven sizes (sides 128-512 at 0.5 mm)
     cut from the 256^3 MR at seeded 6-DOF poses, `stack_poses` candidate
@@ -530,6 +598,9 @@ def main():
     small = None
     if rank == 0 and not args.no_small:
         small = small_configs(local)
+    fixed = None
+    if rank == 0 and not args.no_fixed:
+        fixed = fixed_leg(args, case, local)
     stack = None
     if rank == 0 and not args.no_stack:
         stack = stack_leg(args, case, local)
@@ -556,6 +627,7 @@ def main():
                       "batched_over_plain": value / world / plain_eps},
             "reference_gpu_kernels": ref_gpu,
             "small_configs": small,
+            "fixed_modality": fixed,
             "stack": stack,
             "serve": serve,
             "gpu_launches": launches,
