@@ -556,6 +556,9 @@ int launch_group_generic(lc2_context* c, int k0, int cnt, float* osig, float* om
 
 // The fused kernel (static ultrasound): one launch for `cnt` transforms.
 int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
+  if (!c->cfg.high_res_is_moving || !c->d_sigma || !c->d_su)
+    return fail(LC2_ERR_INVALID_ARGUMENT, "the static-ultrasound kernel needs a context with "
+                "HighResolutionModality: Moving");
   lc2::FusedLaunch L;
   L.mov = c->d_moving;
   L.ust = c->d_static;
@@ -598,6 +601,9 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
 // joint histogram, entropies; results straight into d_out.
 // The fused kernel of a resampled ultrasound: one launch for `cnt` transforms.
 int launch_fused_fixed(lc2_context* c, int k0, int cnt) {
+  if (c->cfg.high_res_is_moving || !c->d_fq || !c->d_fs || !c->d_fd)
+    return fail(LC2_ERR_INVALID_ARGUMENT, "the resampled-ultrasound kernel needs a context with "
+                "HighResolutionModality: Fixed");
   lc2::FixedLaunch L;
   L.mov = c->d_moving;
   L.S = lc2::FixedStatic{c->d_fq, c->d_fs, c->d_fd, c->nv};
@@ -614,6 +620,7 @@ int launch_fused_fixed(lc2_context* c, int k0, int cnt) {
     L.tile_height = 16;
   L.zchunk = c->zchunk;
   L.stream = c->stream;
+  TimerScope ts(c, K_MOMENTS);
   cudaError_t e;
   switch (c->cfg.storage) {
     case LC2_STORE_F16: e = lc2::fixed_launch<__half>(L); break;
@@ -1341,7 +1348,7 @@ int enqueue_batch(lc2_context* c, int count) {
     LC2_TRY(launch_mi(c, count));
   } else {
     LC2_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2 * count, c->stream));
-    LC2_TRY(launch_fused(c, 0, count, nullptr));
+    LC2_TRY(launch_group(c, 0, count));
     LC2_TRY(launch_finalize(c, count));
   }
   LC2_CUDA(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(double) * count, cudaMemcpyDeviceToHost,
@@ -1442,7 +1449,9 @@ int lc2_evaluate_batch(lc2_context* c, const float* matrices, int count, double*
   g_err.clear();
   LC2_TRY(check_ctx(c));
   if (count > 0 && !out) return fail(LC2_ERR_INVALID_ARGUMENT, "null output");
-  if ((c->cfg.high_res_is_moving || c->mi) && c->use_graphs && !c->timing && count > 0) {
+  // every fused path (either modality) and mutual information replay a graph;
+  // the generic path's launches depend on its scratch slots
+  if (!c->generic && c->use_graphs && !c->timing && count > 0) {
     LC2_TRY(select_device(c));
     LC2_TRY(stage_host(c, matrices, count));
     c->staged = count;

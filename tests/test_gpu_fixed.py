@@ -125,3 +125,16 @@ def test_fixed_2d_wide_perturbations_match_oracle():
             continue
         assert abs(fused[k] / ref - 1.0) < REL_LC2, (k, fused[k], ref)
         assert abs(generic[k] / ref - 1.0) < REL_LC2, (k, generic[k], ref)
+
+
+def test_fixed_replays_graphs_generic_does_not():
+    case, mats = _fixed("3d", 3)
+    ctx = make_context(case)
+    first = ctx.evaluate_batch(mats)  # captured
+    g0 = ctx.graph_launches()
+    assert np.array_equal(ctx.evaluate_batch(mats), first)
+    assert ctx.graph_launches() == g0 + 1
+    ctx.set_option(capi.OPTION_GENERIC, 1)
+    g1 = ctx.graph_launches()
+    ctx.evaluate_batch(mats)
+    assert ctx.graph_launches() == g1
