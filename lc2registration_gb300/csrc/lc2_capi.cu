@@ -1420,9 +1420,9 @@ int lc2_launch_staged(lc2_context* c, int count) {
   LC2_TRY(select_device(c));
   if (c->mi) return launch_mi(c, count);
   LC2_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2 * count, c->stream));
-  // the fused path keeps nothing per transform on the device, so one launch
+  // the fused paths keep nothing per transform on the device, so one launch
   // covers the whole batch; the generic path is bounded by its scratch slots
-  const int group = c->cfg.high_res_is_moving ? count : c->slots;
+  const int group = c->generic ? c->slots : count;
   for (int k0 = 0; k0 < count; k0 += group) {
     int cnt = std::min(group, count - k0);
     LC2_TRY(launch_group(c, k0, cnt));

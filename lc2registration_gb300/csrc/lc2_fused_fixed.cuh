@@ -191,6 +191,16 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
   //   2: x window pass; sampling base of slice e+1;
   //   3: y window pass into Y.
   bool pending = false;  // Y holds the patch sums of output slice z-1
+  int nqm[MAXP], nqg[MAXP];  // static qM, qG of the next entering slice
+#pragma unroll
+  for (int j = 0; j < MAXP; ++j) {
+    nqm[j] = nqg[j] = 0;
+    if (pin[j] && e0 >= 0 && e0 < P.vz) {
+      const size_t gi = (size_t)e0 * slice + pu[j];
+      nqm[j] = __ldg(S.q + gi);
+      nqg[j] = __ldg(S.q + S.nv + gi);
+    }
+  }
   for (int e = e0; e < ze + R; ++e) {
     const int z = e - R;          // output slice completed by this entering slice
     const int l = e - 2 * R - 1;  // slice leaving the window
@@ -212,11 +222,8 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
         } else if (pin[j] && zin) {
           u = fused_sample<3, TM>(mov, P, s_A, s_ib, s_fb, ppx[j], ppy[j]);
         }
-        if (pin[j] && zin) {
-          const size_t gi = (size_t)e * slice + pu[j];
-          qm = __ldg(S.q + gi);
-          qg = __ldg(S.q + S.nv + gi);
-        }
+        qm = nqm[j];
+        qg = nqg[j];
         const int qu = quant(u, P.qu), inv = (u > 1e-6f) ? 0 : 1;
         rin[p] = 2 * qu + inv;
         rin[G::NP + p] = qm;
@@ -236,6 +243,18 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
           sUG[j] -= (long long)qul * qgl;
         }
         if (out) fixed_limbs(A + pa_off[j], PA, sU[j], sI[j], sUU[j], sUM[j], sUG[j], P.kbits);
+      }
+    }
+    {
+      const bool zn = (e + 1 >= 0 && e + 1 < P.vz);
+#pragma unroll
+      for (int j = 0; j < MAXP; ++j) {
+        nqm[j] = nqg[j] = 0;
+        if (pin[j] && zn) {
+          const size_t gi = (size_t)(e + 1) * slice + pu[j];
+          nqm[j] = __ldg(S.q + gi);
+          nqg[j] = __ldg(S.q + S.nv + gi);
+        }
       }
     }
     __syncthreads();
