@@ -104,3 +104,26 @@ def test_register_yaml_3d(tmp_path):
     _check_files(tmp_path, result, params, sim, evals,
                  ["TX", "TY", "TZ", "RX", "RY", "RZ", "ScaleX", "ScaleY", "ScaleZ", "ShearX",
                   "ShearY", "ShearZ"], "3D", case)
+
+
+def test_register_yaml_3d_fixed_modality(tmp_path):
+    """HighResolutionModality: Fixed -- the mode of the reference's own 3D
+    config: the MR is the fixed (static, high-resolution) volume and the
+    ultrasound is warped. The parameter-file flow equals lc2_register called
+    directly, on the fused kernel of that modality."""
+    base = synth.case_3d(seed=5, mr_size=40, us_size=32, r=2, blobs=6)
+    case = synth.Case(base.mode, base.moving_geom, base.moving, base.fixed_geom, base.fixed,
+                      list(base.moving_geom.spacing), base.r, hr_moving=False, true_params={},
+                      true_mat=np.linalg.inv(base.true_mat.astype(np.float64)).astype(np.float32))
+    lo = np.array([-10, -10, -10, -8, -8, -8, 0.9, 0.9, 0.9, -0.05, -0.05, -0.05])
+    hi = -lo.copy()
+    hi[6:9] = 1.1
+    assert "HighResolutionModality: Fixed" in open(
+        write_param_file(tmp_path, case, rounds=ROUNDS)).read()
+    params, sim, evals, result, ref = _run(tmp_path, "3D", case, lo, hi)
+    np.testing.assert_allclose(params, ref["params"], rtol=1e-7, atol=1e-7)
+    assert abs(sim / ref["lc2"] - 1) < 1e-7 and evals == ref["evaluations"]
+    assert sim > 0.0
+    _check_files(tmp_path, result, params, sim, evals,
+                 ["TX", "TY", "TZ", "RX", "RY", "RZ", "ScaleX", "ScaleY", "ScaleZ", "ShearX",
+                  "ShearY", "ShearZ"], "3D", case)
