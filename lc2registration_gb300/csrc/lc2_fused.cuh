@@ -72,6 +72,27 @@ struct FusedGeom {
   static constexpr size_t BYTES = OFF_A + sizeof(int) * (size_t)kLimbs * HY * HXP;
 };
 
+// Halo point q of a 2D tile -> (hy, hx): the first 32 columns row by row,
+// one row per warp, then the 2R-column tail row by row. A warp's plane reads
+// and limb writes are then 32 consecutive words (row-major numbering over the
+// 32+2R wide halo put a row break inside most warps: 33-40 words, two lanes on
+// one bank), which pays in the shared-memory-bound 2D kernels (+3.6 %). The
+// 3D kernels keep row-major numbering: there the tail warps' global loads of
+// the static fields would span four rows. Every sum is exact, so the
+// assignment does not change results.
+template <int HX, int HY>
+__device__ __forceinline__ void halo_coord(int q, int& hy, int& hx) {
+  constexpr int MAIN = 32 * HY, TW = HX - 32;
+  if (q < MAIN) {
+    hy = q >> 5;
+    hx = q & 31;
+  } else {
+    const int t = q - MAIN;
+    hy = t / TW;
+    hx = 32 + (t - hy * TW);
+  }
+}
+
 // Trilinear / bilinear sample of the moving image at region point (px, py)
 // of the current slice; sb/sf: integer part and fraction of the region base.
 template <int WND, typename TM>
@@ -443,7 +464,8 @@ __device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
   }
   __syncthreads();
   for (int p = tid; p < G::NP; p += NT) {
-    const int hy = p / G::HX, hx = p - hy * G::HX;
+    int hy, hx;
+    halo_coord<G::HX, G::HY>(p, hy, hx);
     const int gx = x0 - R + hx, gy = y0 - R + hy;
     const int c = (hy + 1) * G::PW + hx + 1;
     const float m = mc[c];

@@ -309,7 +309,8 @@ __global__ void __launch_bounds__(512, 3)
   __syncthreads();
   const bool inside = T.inside;
   for (int p = tid; p < G::NP; p += NT) {
-    const int hy = p / G::HX, hx = p - hy * G::HX;
+    int hy, hx;
+    halo_coord<G::HX, G::HY>(p, hy, hx);
     const int gx = x0 - R + hx, gy = y0 - R + hy;
     const bool pin = gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy;
     float u = 0.0f;
