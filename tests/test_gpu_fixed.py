@@ -138,3 +138,52 @@ def test_fixed_replays_graphs_generic_does_not():
     g1 = ctx.graph_launches()
     ctx.evaluate_batch(mats)
     assert ctx.graph_launches() == g1
+
+
+def test_fixed_odd_sizes_and_tiny_grids():
+    from lc2registration_gb300 import synth
+    from lc2registration_gb300.geometry import Geometry
+
+    rng = np.random.default_rng(19)
+    for (nx, ny, nz, r) in [(7, 5, 3, 1), (33, 9, 11, 2), (65, 17, 1, 4), (41, 23, 19, 5)]:
+        mode = "3D" if nz > 1 else "2D"
+        g = Geometry((nx, ny, nz), (1, 1, 1), (0, 0, 0))
+        mov = (rng.random((nz, ny, nx)) + 0.2).astype(np.float32)
+        fix = rng.random((nz, ny, nx)).astype(np.float32)
+        vs = [1.0, 1.0, 1.0][: (3 if mode == "3D" else 2)]
+        case = synth.Case(mode, g, fix, g, mov, vs, r, False, {}, None)
+        mat = np.eye(4 if mode == "3D" else 3, dtype=np.float32)
+        mat[0, -1] = 0.37
+        ctx = make_context(case)
+        got = ctx.evaluate(mat)
+        ref = oracle_eval(case, mat, use_boxsum=False)
+        if ref == 0.0:
+            assert got == 0.0
+        else:
+            assert abs(got / ref - 1.0) < REL_LC2, (nx, ny, nz, r, got, ref)
+
+
+@pytest.mark.parametrize("hr_moving", [True, False])
+def test_anisotropic_spacings_match_oracle(hr_moving):
+    """Fixed, moving and virtual spacings all different and anisotropic, so
+    the virtual grid is neither image's grid."""
+    from lc2registration_gb300 import synth
+    from lc2registration_gb300.geometry import Geometry, affine3d
+
+    rng = np.random.default_rng(23)
+    fg = Geometry((30, 26, 22), (1.1, 0.9, 1.3), (2.0, -1.0, 0.5))
+    mg = Geometry((36, 34, 30), (0.95, 1.05, 0.85), (0.0, 0.0, 0.0))
+    mr = synth.mr_phantom((30, 34, 36), 6, 1.2, seed=41)
+    us = (rng.random((22, 26, 30)) * 0.2 + 0.3).astype(np.float32)
+    if hr_moving:
+        case = synth.Case("3D", fg, us, mg, mr, [1.2, 0.8, 1.0], 2, True, {}, None)
+    else:
+        case = synth.Case("3D", mg, mr, fg, us, [1.2, 0.8, 1.0], 2, False, {}, None)
+    mats = [affine3d((2.0, -1.5, 1.0), (0.7, -0.4, 0.3), (1.02, 0.98, 1.0), (0.01, 0.0, -0.01),
+                     (15.0, 14.0, 13.0), (0, 0, 0)).astype(np.float32)]
+    ctx = make_context(case)
+    for m in mats:
+        got = ctx.evaluate(m)
+        ref = oracle_eval(case, m, use_boxsum=False)
+        assert ref > 0.0
+        assert abs(got / ref - 1.0) < REL_LC2, (got, ref)
