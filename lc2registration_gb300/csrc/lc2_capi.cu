@@ -162,6 +162,7 @@ struct lc2_context {
   int* d_fs = nullptr;
   long long* d_fd = nullptr;
   int generic = 0;  // LC2_OPTION_GENERIC
+  int sms = 152;    // multiprocessors of the device (queried at creation)
   // normalised mutual information (patch_size 0): static image bins and
   // entropy, per-transform range and joint histogram
   bool mi = false;
@@ -581,6 +582,7 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
   L.zchunk = c->zchunk;
   L.pipeline = c->pipeline;
   L.err = c->d_err;
+  L.sms = c->sms;
   L.stream = c->stream;
   cudaError_t e;
   {
@@ -619,6 +621,7 @@ int launch_fused_fixed(lc2_context* c, int k0, int cnt) {
       (long long)((c->virt.dim[0] + 31) / 32) * ((c->virt.dim[1] + 7) / 8) > 65535)
     L.tile_height = 16;
   L.zchunk = c->zchunk;
+  L.sms = c->sms;
   L.stream = c->stream;
   TimerScope ts(c, K_MOMENTS);
   cudaError_t e;
@@ -838,6 +841,9 @@ int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
     delete c;
     return fail(LC2_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
   }
+  if (cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, cfg->device) != cudaSuccess ||
+      c->sms < 1)
+    c->sms = 152;
   c->stream = c->own_stream;
   e = dev_alloc((void**)&c->d_scratch, c->per_slot * c->slots, c->stream);
   c->owns_moving = own_moving;

@@ -772,6 +772,30 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
   if ((tid & 31) == 0) atomicAdd(acc + 2 * (size_t)(k0 + slot), (unsigned long long)acc_m);
 }
 
+// Output slices per CTA of a 3D launch left automatic: the z split with
+// the smallest modelled makespan, waves x (chunk + 2R) -- a CTA streams its
+// chunk plus 2R warm-up slices, `slots` CTAs run at once -- among chunks of
+// at least 4R + 4 slices. One transform at 256^3 then runs as one wave of
+// whole-depth columns rather than five waves of 52-slice chunks.
+inline int auto_zchunk(int vz, int R, long long tiles, long long slots) {
+  int cap = vz / (4 * R + 4);
+  cap = cap < 1 ? 1 : cap;
+  slots = slots < 1 ? 1 : slots;
+  long long best = -1;
+  int best_zc = vz;
+  for (int nz = 1; nz <= cap; ++nz) {
+    const int zc = (vz + nz - 1) / nz;
+    const long long chunks = (vz + zc - 1) / zc;
+    const long long waves = (tiles * chunks + slots - 1) / slots;
+    const long long cost = waves * (zc + 2 * R);
+    if (best < 0 || cost < best) {
+      best = cost;
+      best_zc = zc;
+    }
+  }
+  return best_zc;
+}
+
 // Launch description shared by the per-storage-type launchers.
 struct FusedLaunch {
   const void* mov;
@@ -788,6 +812,7 @@ struct FusedLaunch {
   int zchunk;       // 3D: output slices per CTA; 0 = automatic
   int pipeline;     // 3D, radius <= 4, no per-voxel output: warp-specialised kernel
   int* err;         // device flag raised by the warp-specialised kernel's bounded waits
+  int sms;          // multiprocessors of the device
   cudaStream_t stream;
 };
 
@@ -806,12 +831,8 @@ cudaError_t fused_launch_rt(const FusedLaunch& L) {
     P.zchunk = L.zchunk < P.vz ? L.zchunk : P.vz;
     nz = (P.vz + P.zchunk - 1) / P.zchunk;
   } else if (ND == 3) {
-    const long long ctas = (long long)ntx * nty * L.cnt;
-    nz = (int)((4LL * 152 + ctas - 1) / ctas);
-    nz = nz < 1 ? 1 : nz;
-    const int cap = P.vz / (4 * R + 4);
-    nz = nz > (cap < 1 ? 1 : cap) ? (cap < 1 ? 1 : cap) : nz;
-    P.zchunk = (P.vz + nz - 1) / nz;
+    P.zchunk = auto_zchunk(P.vz, R, (long long)ntx * nty * L.cnt,
+                           (long long)L.sms * fused_min_blocks(3, TY, R));
     nz = (P.vz + P.zchunk - 1) / P.zchunk;
   } else {
     P.zchunk = 1;

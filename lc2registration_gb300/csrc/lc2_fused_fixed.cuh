@@ -352,6 +352,7 @@ struct FixedLaunch {
   int nd, wnd;
   int tile_height;  // 3D, radius <= 4: 16 or 8 rows per tile
   int zchunk;       // 3D: output slices per CTA; 0 = automatic
+  int sms;          // multiprocessors of the device
   cudaStream_t stream;
 };
 
@@ -365,19 +366,12 @@ cudaError_t fixed_launch3(const FixedLaunch& L) {
   FusedParams P = L.P;
   const int ntx = (P.vx + 31) / 32, nty = (P.vy + TY - 1) / TY;
   P.ntx = ntx;
-  int nz;
-  if (L.zchunk > 0) {
+  if (L.zchunk > 0)
     P.zchunk = L.zchunk < P.vz ? L.zchunk : P.vz;
-  } else {
-    const long long ctas = (long long)ntx * nty * L.cnt;
-    nz = (int)((4LL * 152 + ctas - 1) / ctas);
-    nz = nz < 1 ? 1 : nz;
-    int cap = P.vz / (4 * R + 4);
-    cap = cap < 1 ? 1 : cap;
-    nz = nz > cap ? cap : nz;
-    P.zchunk = (P.vz + nz - 1) / nz;
-  }
-  nz = (P.vz + P.zchunk - 1) / P.zchunk;
+  else
+    P.zchunk = auto_zchunk(P.vz, R, (long long)ntx * nty * L.cnt,
+                           (long long)L.sms * fused_min_blocks(3, TY, R));
+  const int nz = (P.vz + P.zchunk - 1) / P.zchunk;
   dim3 grid(L.cnt, ntx * nty, nz);
   kern<<<grid, 32 * TY, F::BYTES, L.stream>>>((const T*)L.mov, L.S, P, L.xf, L.k0, L.acc);
   return cudaGetLastError();

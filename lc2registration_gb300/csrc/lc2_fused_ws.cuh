@@ -289,12 +289,7 @@ cudaError_t fused_ws_launch_r(const FusedLaunch& L, int* err) {
   if (L.zchunk > 0) {
     P.zchunk = L.zchunk < P.vz ? L.zchunk : P.vz;
   } else {
-    const long long ctas = (long long)ntx * nty * L.cnt;
-    nz = (int)((4LL * 152 + ctas - 1) / ctas);
-    nz = nz < 1 ? 1 : nz;
-    const int cap = P.vz / (4 * R + 4);
-    nz = nz > (cap < 1 ? 1 : cap) ? (cap < 1 ? 1 : cap) : nz;
-    P.zchunk = (P.vz + nz - 1) / nz;
+    P.zchunk = auto_zchunk(P.vz, R, (long long)ntx * nty * L.cnt, (long long)L.sms);
   }
   nz = (P.vz + P.zchunk - 1) / P.zchunk;
   dim3 grid(L.cnt, ntx * nty, nz);
