@@ -316,6 +316,7 @@ def small_configs(device):
         plain_eps = len(plain) / (time.perf_counter() - t0)
         assert np.array_equal(np.array(plain), vals[:len(plain)]), "plain != batched"
         out[name] = {"batched_evals_per_s": batched, "plain_evals_per_s": plain_eps,
+                     "plain_latency_ms": 1e3 / plain_eps,
                      "batched_over_plain": batched / plain_eps, "candidates_per_launch": K,
                      "virtual_voxels": int(np.prod(ctx.virtual_dims())), "storage": "f32"}
         ctx.close()
