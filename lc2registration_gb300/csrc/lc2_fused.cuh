@@ -375,6 +375,34 @@ __device__ __forceinline__ float fused_sobel_sd(const float2* SD, int c) {
   return sqrt_approx(gx * gx + gy * gy + gz * gz);
 }
 
+// Sampling base of a tile's PW x PH resampled region at slice zs: the
+// moving-pixel coordinate of the canonical base, region row -yb (yb = 0 in
+// 2D), split into integer part ib and fraction fb (xform_coord); returns
+// whether the region lies in the virtual grid (origin gx0, gy0; zin: the
+// slice is in the grid) with every sample of it strictly inside the moving
+// image along its first WND axes (0 <= floor, floor + 1 <= dim - 1; the
+// region's corners bound the affine image, 0.01 voxel covers float rounding).
+template <int WND, int PW, int PH>
+__device__ __forceinline__ bool region_base(const Xform& X, const float* A, const FusedParams& P,
+                                            int gx0, int gy0, int yb, int zs, bool zin,
+                                            int* ib, float* fb) {
+  bool in = zin && gx0 >= 0 && gx0 + PW <= P.vx && gy0 >= 0 && gy0 + PH <= P.vy;
+  const int dims[3] = {P.mx, P.my, P.mz};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    xform_coord(X, a, gx0, gy0 - yb, zs, ib[a], fb[a]);
+    if (a < WND) {
+      const float ex = A[3 * a] * (float)(PW - 1);
+      const float e0 = A[3 * a + 1] * (float)yb, e1 = A[3 * a + 1] * (float)(yb + PH - 1);
+      const float lo = fb[a] + fminf(ex, 0.0f) + fminf(e0, e1);
+      const float hi = fb[a] + fmaxf(ex, 0.0f) + fmaxf(e0, e1);
+      in = in && ((float)ib[a] + lo >= 0.01f) &&
+           ((float)ib[a] + hi <= (float)(dims[a] - 1) - 0.01f);
+    }
+  }
+  return in;
+}
+
 // Per-tile transform state in shared memory.
 struct TileShared {
   int ib[3];       // resampled-region origin in moving pixels: integer part
@@ -426,22 +454,8 @@ __device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
   const int gx0 = x0 - R - 1, gy0 = y0 - R - 1;
   if (tid == 0) {
 #pragma unroll
-    for (int a = 0; a < 3; ++a) xform_coord(*X, a, gx0, gy0, 0, T.ib[a], T.fb[a]);
-#pragma unroll
     for (int i = 0; i < 9; ++i) T.A[i] = X->ah[i];
-    // region in the virtual grid and every sample strictly inside the moving
-    // image (corners bound the affine image; 0.01 voxel covers float rounding)
-    bool in = gx0 >= 0 && gx0 + G::PW <= P.vx && gy0 >= 0 && gy0 + G::PH <= P.vy;
-    const int dims[3] = {P.mx, P.my, P.mz};
-#pragma unroll
-    for (int a = 0; a < WND; ++a) {
-      const float ex = T.A[3 * a] * (float)(G::PW - 1), ey = T.A[3 * a + 1] * (float)(G::PH - 1);
-      const float lo = T.fb[a] + fminf(ex, 0.0f) + fminf(ey, 0.0f);
-      const float hi = T.fb[a] + fmaxf(ex, 0.0f) + fmaxf(ey, 0.0f);
-      in = in && ((float)T.ib[a] + lo >= 0.01f) &&
-           ((float)T.ib[a] + hi <= (float)(dims[a] - 1) - 0.01f);
-    }
-    T.inside = in ? 1 : 0;
+    T.inside = region_base<WND, G::PW, G::PH>(*X, T.A, P, gx0, gy0, 0, 0, true, T.ib, T.fb) ? 1 : 0;
   }
   __syncthreads();
   if (T.inside) {
@@ -543,24 +557,10 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
   // fraction for the float per-point offsets; run by the last thread, whose
   // warp holds the fewest halo points
   auto set_base = [&](int zs) {
-    if (tid == NT - 1) {
-      // the region lies in the virtual grid and every sample of it strictly
-      // inside the moving volume (0 <= floor, floor + 1 <= dim - 1; corners of
-      // the region bound the affine image, 0.01 voxel covers float rounding)
-      bool in = ND == 3 && zs >= 0 && zs < P.vz && gx0 >= 0 && gx0 + G::PW <= P.vx &&
-                gy0 >= 0 && gy0 + G::PH <= P.vy;
-      const int dims[3] = {P.mx, P.my, P.mz};
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        xform_coord(s_xf, a, gx0, gy0 - yb, zs, s_ib[a], s_fb[a]);
-        const float ex = s_A[3 * a] * (float)(G::PW - 1);
-        const float e0 = s_A[3 * a + 1] * (float)yb, e1 = s_A[3 * a + 1] * (float)(yb + G::PH - 1);
-        const float lo = s_fb[a] + fminf(ex, 0.0f) + fminf(e0, e1);
-        const float hi = s_fb[a] + fmaxf(ex, 0.0f) + fmaxf(e0, e1);
-        in = in && ((float)s_ib[a] + lo >= 0.01f) && ((float)s_ib[a] + hi <= (float)(dims[a] - 1) - 0.01f);
-      }
-      s_inside = in ? 1 : 0;
-    }
+    if (tid == NT - 1)
+      s_inside = region_base<3, G::PW, G::PH>(s_xf, s_A, P, gx0, gy0, yb, zs,
+                                              ND == 3 && zs >= 0 && zs < P.vz, s_ib, s_fb)
+                     ? 1 : 0;
   };
   if (tid == 0) {
     s_xf = *X;

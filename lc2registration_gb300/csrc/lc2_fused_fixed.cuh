@@ -132,22 +132,10 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
   const size_t slice = (size_t)P.vx * P.vy;
 
   auto set_base = [&](int zs) {
-    if (tid == NT - 1) {
-      bool in = zs >= 0 && zs < P.vz && gx0 >= 0 && gx0 + G::PW <= P.vx && gy0 >= 0 &&
-                gy0 + G::PH <= P.vy;
-      const int dims[3] = {P.mx, P.my, P.mz};
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        xform_coord(s_xf, a, gx0, gy0 - yb, zs, s_ib[a], s_fb[a]);
-        const float ex = s_A[3 * a] * (float)(G::PW - 1);
-        const float ea = s_A[3 * a + 1] * (float)yb, eb = s_A[3 * a + 1] * (float)(yb + G::PH - 1);
-        const float lo = s_fb[a] + fminf(ex, 0.0f) + fminf(ea, eb);
-        const float hi = s_fb[a] + fmaxf(ex, 0.0f) + fmaxf(ea, eb);
-        in = in && ((float)s_ib[a] + lo >= 0.01f) &&
-             ((float)s_ib[a] + hi <= (float)(dims[a] - 1) - 0.01f);
-      }
-      s_inside = in ? 1 : 0;
-    }
+    if (tid == NT - 1)
+      s_inside = region_base<3, G::PW, G::PH>(s_xf, s_A, P, gx0, gy0, yb, zs,
+                                              zs >= 0 && zs < P.vz, s_ib, s_fb)
+                     ? 1 : 0;
   };
   if (tid == 0) {
     s_xf = *X;
@@ -291,20 +279,8 @@ __global__ void __launch_bounds__(512, 3)
   const int gx0 = x0 - R - 1, gy0 = y0 - R - 1;
   if (tid == 0) {
 #pragma unroll
-    for (int a = 0; a < 3; ++a) xform_coord(*X, a, gx0, gy0, 0, T.ib[a], T.fb[a]);
-#pragma unroll
     for (int i = 0; i < 9; ++i) T.A[i] = X->ah[i];
-    bool in = gx0 >= 0 && gx0 + G::PW <= P.vx && gy0 >= 0 && gy0 + G::PH <= P.vy;
-    const int dims[3] = {P.mx, P.my, P.mz};
-#pragma unroll
-    for (int a = 0; a < WND; ++a) {
-      const float ex = T.A[3 * a] * (float)(G::PW - 1), ey = T.A[3 * a + 1] * (float)(G::PH - 1);
-      const float lo = T.fb[a] + fminf(ex, 0.0f) + fminf(ey, 0.0f);
-      const float hi = T.fb[a] + fmaxf(ex, 0.0f) + fmaxf(ey, 0.0f);
-      in = in && ((float)T.ib[a] + lo >= 0.01f) &&
-           ((float)T.ib[a] + hi <= (float)(dims[a] - 1) - 0.01f);
-    }
-    T.inside = in ? 1 : 0;
+    T.inside = region_base<WND, G::PW, G::PH>(*X, T.A, P, gx0, gy0, 0, 0, true, T.ib, T.fb) ? 1 : 0;
   }
   __syncthreads();
   const bool inside = T.inside;
