@@ -363,8 +363,10 @@ def fixed_leg(args, main_case, device):
         case = swapped(base)
         mats = np.linalg.inv(perturbed(base, np.random.default_rng(3), K).astype(np.float64))
         mats = mats.astype(np.float32)
+        # max_batch 16: the generic path batches 16 transforms per group (its
+        # scratch holds one warped image per transform); the fused path needs none
         ctx = capi.Context(case.mode, case.fixed_geom, case.moving_geom, case.virt_spacing, case.r,
-                           False, storage, device=device)
+                           False, storage, 16, device=device)
         ctx.set_images(case.fixed, case.moving)
         ctx.stage(mats)
         fused = timed(ctx, K, 5)

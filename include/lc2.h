@@ -59,7 +59,10 @@ typedef struct {
                               * 0 = normalised mutual information (3D) */
     int high_res_is_moving;  /* HighResolutionModality: 1 = Moving, 0 = Fixed */
     int storage;             /* lc2_storage */
-    int max_batch;           /* transforms per launch group; 0 = automatic */
+    int max_batch;           /* transforms per launch group of the generic kernels
+                              * (LC2_OPTION_GENERIC; each holds one warped image of
+                              * scratch); 0 = one. The fused kernels take any batch
+                              * in one launch. */
     int device;              /* CUDA device ordinal */
 } lc2_config;
 

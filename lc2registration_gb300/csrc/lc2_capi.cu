@@ -791,15 +791,12 @@ int plan_context(const lc2_config* cfg, lc2_context* c) {
   int b = 0;
   while (b < 21 && ((long long)c->n << (b + 2)) <= (1LL << 31)) ++b;
   c->qbits = b;
-  // scratch slots: warped image (+ its Sobel when the moving image is the
-  // high-resolution one). The fused path (static ultrasound) keeps nothing
-  // per transform and needs one slot; the generic path takes as many as fit
-  // 1 GiB unless max_batch says more.
+  // scratch slots of the generic path: warped image (+ its Sobel when the
+  // moving image is the high-resolution one). Both fused paths keep nothing
+  // per transform, so one slot (for the field dumps and LC2_OPTION_GENERIC)
+  // unless max_batch asks for more generic-path batching.
   c->per_slot = c->nv * sizeof(float) * (cfg->high_res_is_moving ? 2 : 1);
-  long long slots = cfg->max_batch > 0 ? cfg->max_batch
-                    : cfg->high_res_is_moving
-                        ? 1
-                        : std::max<long long>(1, (1LL << 30) / (long long)c->per_slot);
+  long long slots = cfg->max_batch > 0 ? cfg->max_batch : 1;
   slots = std::min<long long>(slots, 1024);
   slots = std::min<long long>(slots, 65535 / c->virt.dim[2]);
   c->slots = (int)std::max<long long>(1, slots);
