@@ -1,7 +1,7 @@
 """The request loop on the GPU: a mixed stream of 2D, 3D and 2D-to-3D
-registrations submitted at random times runs concurrently (each on its own
-context and stream), and every result equals, bit for bit, the same
-registration run alone."""
+registrations, in both HighResolutionModality settings, submitted at random
+times runs concurrently (each on its own context and stream), and every
+result equals, bit for bit, the same registration run alone."""
 import time
 
 import numpy as np
@@ -27,9 +27,20 @@ def _reg(case):
                 rounds=[(["translation", "rotation"], 1e-3)])
 
 
+def _fixed_roles(case):
+    """HighResolutionModality: Fixed: the MR is the fixed image, the
+    ultrasound is warped."""
+    nd = 2 if case.mode == "2D" else 3
+    return synth.Case(case.mode, case.moving_geom, case.moving, case.fixed_geom, case.fixed,
+                      list(case.moving_geom.spacing[:nd]), case.r, hr_moving=False,
+                      true_params={}, true_mat=None)
+
+
 def _mix():
     cases = [synth.case_2d(seed=s, size=96, r=3) for s in (11, 12, 13)]
     cases += [synth.case_3d(seed=s, mr_size=40, us_size=32, r=2, blobs=6) for s in (14, 15)]
+    cases += [_fixed_roles(synth.case_2d(seed=18, size=96, r=3)),
+              _fixed_roles(synth.case_3d(seed=19, mr_size=40, us_size=32, r=2, blobs=6))]
     mr = synth.mr_phantom((48, 48, 48), 8, 1.5, seed=16)
     mg = Geometry((48, 48, 48), (1.0, 1.0, 1.0), (0.0, 0.0, 0.0))
     cases += synth.frame_stack(mr, mg, 2, seed=17, sides=(40, 56), spacing=0.5, r=3)
