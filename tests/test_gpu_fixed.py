@@ -187,3 +187,26 @@ def test_anisotropic_spacings_match_oracle(hr_moving):
         ref = oracle_eval(case, m, use_boxsum=False)
         assert ref > 0.0
         assert abs(got / ref - 1.0) < REL_LC2, (got, ref)
+
+
+def test_fixed_2dto3d_matches_oracle_and_generic():
+    """2D-to-3D with HighResolutionModality: Fixed: the frame is the static
+    high-resolution image and the volume is sampled trilinearly per
+    transform (k_fused_fixed2 with 3D sampling)."""
+    base = _case("2dto3d")
+    from lc2registration_gb300 import synth
+
+    case = synth.Case(base.mode, base.fixed_geom, base.fixed, base.moving_geom, base.moving,
+                      base.virt_spacing, base.r, hr_moving=False, true_params={},
+                      true_mat=base.true_mat)
+    mats = np.concatenate([case.true_mat[None],
+                           perturbed(base, np.random.default_rng(8), 3, scale=0.5)])
+    ctx = make_context(case)
+    fused = ctx.evaluate_batch(mats)
+    ctx.set_option(capi.OPTION_GENERIC, 1)
+    generic = ctx.evaluate_batch(mats)
+    for k in range(len(mats)):
+        ref = oracle_eval(case, mats[k], use_boxsum=False)
+        assert ref > 0.0
+        assert abs(fused[k] / ref - 1.0) < REL_LC2, (k, fused[k], ref)
+        assert abs(generic[k] / ref - 1.0) < REL_LC2, (k, generic[k], ref)
