@@ -163,11 +163,36 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
     sUU[j] = sUM[j] = sUG[j] = 0;
   }
   long long acc_m = 0, acc_s = 0;
+  // static fields of the next output voxel solved, loaded a slice ahead
+  int nsm = 0, nsg = 0;
+  long long ndmm = 0, ndgg = 0, ndmg = 0;
+  auto load_static = [&](int z) {
+    const int x = x0 + ox, y = y0 + oy;
+    if (z >= zb && z < ze && x < P.vx && y < P.vy) {
+      const size_t gi = ((size_t)z * P.vy + y) * P.vx + x;
+      nsm = __ldg(S.s + gi);
+      nsg = __ldg(S.s + S.nv + gi);
+      ndmm = __ldg(S.d + gi);
+      ndgg = __ldg(S.d + S.nv + gi);
+      ndmg = __ldg(S.d + 2 * S.nv + gi);
+    }
+  };
   auto solve_out = [&](int z) {
     const int x = x0 + ox, y = y0 + oy;
-    if (x < P.vx && y < P.vy)
-      fixed_solve(P, S, Y + oy * 32 + ox, TY * 32, ((size_t)z * P.vy + y) * P.vx + x, acc_m,
-                  acc_s);
+    const int* a = Y + oy * 32 + ox;
+    constexpr int ls = TY * 32;
+    if (x < P.vx && y < P.vy && a[ls] == 0) {
+      const int su = a[0];
+      const long long uu = (long long)a[3 * ls] * (1LL << P.kbits) + a[2 * ls];
+      const long long um = (long long)a[5 * ls] * (1LL << P.kbits) + a[4 * ls];
+      const long long ug = (long long)a[7 * ls] * (1LL << P.kbits) + a[6 * ls];
+      const long long n = P.n;
+      float sigma, m;
+      solve_centred(n * uu - (long long)su * su, ndmm, ndgg, ndmg, n * um - (long long)su * nsm,
+                    n * ug - (long long)su * nsg, P.thr_var, P.thr_m, P.thr_g, P.sig_scale, sigma, m);
+      acc_m += __float2int_rn(m * P.sum_scale);
+      acc_s += __float2int_rn(sigma * P.sum_scale);
+    }
   };
 
   __syncthreads();  // s_xf, s_A
@@ -196,6 +221,7 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
     const bool leave = (l >= e0);
     const bool zin = (e >= 0 && e < P.vz);
     if (pending) solve_out(z - 1);
+    load_static(z);
     int* rin = ring + ((e - e0) % F::RING) * 3 * G::NP;
     const int* rout = ring + ((l - e0 + F::RING) % F::RING) * 3 * G::NP;
     const bool inside = s_inside;
