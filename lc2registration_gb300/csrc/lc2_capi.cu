@@ -143,6 +143,9 @@ struct lc2_context {
   unsigned long long* d_acc = nullptr;
   double* d_out = nullptr;
   int cap = 0;  // capacity of d_xf/d_acc/d_out (transforms)
+  // d_acc is all zero: k_finalize resets what it read, so only a launch whose
+  // sums were not finalised (another path, an error) leaves it dirty
+  bool acc_clean = false;
   lc2::Xform* h_xf = nullptr;  // pinned staging
   double* h_out = nullptr;     // pinned results
   int staged = 0;
@@ -261,12 +264,17 @@ __global__ void k_fixed_centre(const int* __restrict__ s, long long* __restrict_
 // LC2 = sum(measure) / sum(sigma); 0 when NaN/Inf (cu_lc2_3d.cu:1189-1191).
 // sigma_sum >= 0: the weighting-factor sum is static (precomputed), else it
 // is taken from the accumulator.
-__global__ void k_finalize(const unsigned long long* __restrict__ acc, int count,
+// The sums it read are reset to zero, so a replayed batch starts from zero
+// without a memset.
+__global__ void k_finalize(unsigned long long* __restrict__ acc, int count,
                            double* __restrict__ out, long long sigma_sum) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
-  double m = (double)(long long)acc[2 * k];
-  double s = sigma_sum >= 0 ? (double)sigma_sum : (double)(long long)acc[2 * k + 1];
+  const unsigned long long a0 = acc[2 * k], a1 = acc[2 * k + 1];
+  acc[2 * k] = 0;
+  acc[2 * k + 1] = 0;
+  double m = (double)(long long)a0;
+  double s = sigma_sum >= 0 ? (double)sigma_sum : (double)(long long)a1;
   double v = m / s;
   if (isnan(v) || isinf(v)) v = 0.0;
   out[k] = v;
@@ -379,6 +387,7 @@ int ensure_capacity(lc2_context* c, int count) {
   c->cap = 0;
   LC2_CUDA(dev_alloc((void**)&c->d_xf, sizeof(lc2::Xform) * ncap, c->stream));
   LC2_CUDA(dev_alloc((void**)&c->d_acc, sizeof(unsigned long long) * 2 * ncap, c->stream));
+  c->acc_clean = false;
   LC2_CUDA(dev_alloc((void**)&c->d_out, sizeof(double) * ncap, c->stream));
   LC2_CUDA(host_alloc((void**)&c->h_xf, sizeof(lc2::Xform) * ncap));
   LC2_CUDA(host_alloc((void**)&c->h_out, sizeof(double) * ncap));
@@ -479,6 +488,7 @@ int launch_sobel(lc2_context* c, const float* in, float* out, int cnt, size_t sl
 template <int ND, typename TU>
 int launch_moments_t(lc2_context* c, const TU* U, const float* M, const float* G,
                      const lc2::MomentParams& P, int k0, int cnt, float* osig, float* omeas) {
+  c->acc_clean = false;
   const lc2_geometry& v = c->virt;
   size_t smem = lc2::mom_smem_bytes(P.r);
   LC2_CUDA(cudaFuncSetAttribute(lc2::k_moments<ND, TU>,
@@ -557,6 +567,7 @@ int launch_group_generic(lc2_context* c, int k0, int cnt, float* osig, float* om
 
 // The fused kernel (static ultrasound): one launch for `cnt` transforms.
 int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
+  c->acc_clean = false;
   if (!c->cfg.high_res_is_moving || !c->d_sigma || !c->d_su)
     return fail(LC2_ERR_INVALID_ARGUMENT, "the static-ultrasound kernel needs a context with "
                 "HighResolutionModality: Moving");
@@ -603,6 +614,7 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
 // joint histogram, entropies; results straight into d_out.
 // The fused kernel of a resampled ultrasound: one launch for `cnt` transforms.
 int launch_fused_fixed(lc2_context* c, int k0, int cnt) {
+  c->acc_clean = false;
   if (c->cfg.high_res_is_moving || !c->d_fq || !c->d_fs || !c->d_fd)
     return fail(LC2_ERR_INVALID_ARGUMENT, "the resampled-ultrasound kernel needs a context with "
                 "HighResolutionModality: Fixed");
@@ -863,6 +875,7 @@ int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
     e = dev_alloc((void**)&c->d_fd, 3 * c->nv * sizeof(long long), c->stream);
   if (e == cudaSuccess) e = dev_alloc((void**)&c->d_err, sizeof(int), c->stream);
   if (e == cudaSuccess) e = host_alloc((void**)&c->h_err, sizeof(int));
+  if (e == cudaSuccess) *c->h_err = 0;  // pinned buffers come from a reuse cache
   if (e == cudaSuccess) e = cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
   if (e != cudaSuccess) {
     lc2_destroy(c);
@@ -1350,13 +1363,16 @@ int enqueue_batch(lc2_context* c, int count) {
   if (c->mi) {
     LC2_TRY(launch_mi(c, count));
   } else {
-    LC2_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2 * count, c->stream));
+    // no memset: the sums start at zero (acc_clean, checked before each
+    // replay) and k_finalize resets them
     LC2_TRY(launch_group(c, 0, count));
     LC2_TRY(launch_finalize(c, count));
   }
   LC2_CUDA(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(double) * count, cudaMemcpyDeviceToHost,
                            c->stream));
-  LC2_CUDA(cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  // only the warp-specialised kernel raises the error flag
+  if (c->pipeline)
+    LC2_CUDA(cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   return LC2_OK;
 }
 
@@ -1458,8 +1474,13 @@ int lc2_evaluate_batch(lc2_context* c, const float* matrices, int count, double*
     LC2_TRY(select_device(c));
     LC2_TRY(stage_host(c, matrices, count));
     c->staged = count;
+    if (!c->mi && !c->acc_clean)
+      LC2_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * 2 * (size_t)c->cap,
+                               c->stream));
+    c->acc_clean = false;  // until this batch is known to have finished
     LC2_TRY(launch_batch_graph(c, count));
     LC2_CUDA(cudaStreamSynchronize(c->stream));
+    c->acc_clean = true;  // k_finalize reset every sum the batch used
     LC2_TRY(check_pipeline(c));
     std::memcpy(out, c->h_out, sizeof(double) * count);
     return LC2_OK;
