@@ -323,6 +323,24 @@ def small_configs(device):
     return out
 
 
+def issue_roofline(ipv, voxels, kernel_ms, device, clk):
+    """The bound the fused kernel actually meets: instruction issue. achieved =
+    warp instructions of one launch (ncu's per-voxel count x voxels / 32) per
+    second of the event-timed launch; peak = SMs x 4 schedulers x one warp
+    instruction per cycle at the maximum SM clock sampled."""
+    import torch
+
+    if not ipv or not kernel_ms:
+        return None
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    mhz = (clk.summary() or {}).get("sm_max_mhz") or 2070.0
+    achieved = ipv * voxels / 32.0 / (kernel_ms / 1e3)
+    peak = sms * 4 * mhz * 1e6
+    return {"bound": "issue", "unit": "warp instructions/s", "achieved": achieved, "peak": peak,
+            "frac": achieved / peak,
+            "source": "instructions per voxel from profiles/k_fused_traffic.json (ncu)"}
+
+
 def fixed_leg(args, main_case, device):
     """HighResolutionModality: Fixed (the reference's own configs use it): the
     MR/CT is the static high-resolution image on its own grid and the
@@ -560,10 +578,13 @@ def main():
         except Exception:
             ref_gpu = None
     traffic = None
+    ipv = None  # thread instructions per output voxel of the fused kernel (ncu)
     tfile = os.path.join(ROOT, "profiles", "k_fused_traffic.json")
     if os.path.exists(tfile):
         try:
-            traffic = json.load(open(tfile)).get("bytes_per_launch_scaled")
+            tj = json.load(open(tfile))
+            traffic = tj.get("bytes_per_launch_scaled")
+            ipv = tj.get("thread_instructions_per_voxel")
         except Exception:
             traffic = None
 
@@ -622,6 +643,7 @@ def main():
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "k_fused", "kernel_ms_per_launch": mom_ms / max(1, mom_launches),
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
+            "issue_roofline": issue_roofline(ipv, K * n_vox, mom_ms, local, clk),
             "kernels_ms_per_step": {k: v[0] for k, v in kt.items()},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": K * 96,
