@@ -773,21 +773,19 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
 }
 
 // Output slices per CTA of a 3D launch left automatic: the z split with
-// the smallest modelled makespan, waves x (chunk + 2R) -- a CTA streams its
-// chunk plus 2R warm-up slices, `slots` CTAs run at once -- among chunks of
-// at least 4R + 4 slices. One transform at 256^3 then runs as one wave of
-// whole-depth columns rather than five waves of 52-slice chunks.
+// the smallest modelled makespan, waves x (chunk + 2R + 3) -- a CTA streams
+// its chunk plus 2R warm-up slices after resampling three slices before its
+// loop; `slots` CTAs run at once. One transform at 256^3 runs as one wave of
+// whole-depth columns; one at 96^3 as one wave of 12-slice chunks.
 inline int auto_zchunk(int vz, int R, long long tiles, long long slots) {
-  int cap = vz / (4 * R + 4);
-  cap = cap < 1 ? 1 : cap;
   slots = slots < 1 ? 1 : slots;
   long long best = -1;
   int best_zc = vz;
-  for (int nz = 1; nz <= cap; ++nz) {
+  for (int nz = 1; nz <= vz; ++nz) {
     const int zc = (vz + nz - 1) / nz;
     const long long chunks = (vz + zc - 1) / zc;
     const long long waves = (tiles * chunks + slots - 1) / slots;
-    const long long cost = waves * (zc + 2 * R);
+    const long long cost = waves * (zc + 2 * R + 3);
     if (best < 0 || cost < best) {
       best = cost;
       best_zc = zc;
