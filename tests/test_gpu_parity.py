@@ -238,3 +238,39 @@ def test_degenerate_inputs(kind):
     assert ctx2.evaluate(away) == 0.0
     assert oracle_eval(case, away) == 0.0
     np.testing.assert_array_equal(ctx2.evaluate_batch(np.stack([away, away])), [0.0, 0.0])
+
+
+@pytest.mark.parametrize("hr_moving", [True, False])
+@pytest.mark.parametrize("kind", ["2d", "3d"])
+def test_flat_mr_gives_zero(kind, hr_moving):
+    """A flat MR under the identity, with the ultrasound zero (invalid) in a
+    border band wider than r + 1: every valid patch lies where M is constant
+    and G = 0 (the zero-padded border, where the Sobel sees an edge, only
+    enters invalid patches), so no regressor has variance, every measure is
+    clipped to 0 and LC2 = 0 while sigma > 0 -- on the GPU as in the oracle."""
+    from lc2registration_gb300.geometry import Geometry
+
+    nd = 2 if kind == "2d" else 3
+    dims = (48, 40, 1) if nd == 2 else (40, 36, 32)
+    r = 3 if nd == 2 else 2
+    g = Geometry(dims, (1, 1, 1), (0, 0, 0))
+    rng = np.random.default_rng(31)
+    shape = dims[::-1] if nd == 3 else dims[1::-1]
+    us = (rng.random(shape) * 0.5 + 0.2).astype(np.float32)
+    b = r + 2
+    band = np.ones(shape, dtype=bool)
+    band[tuple(slice(b, n - b) for n in shape)] = False
+    us[band] = 0.0
+    mr = np.full(shape, 0.6, dtype=np.float32)
+    mode = "2D" if nd == 2 else "3D"
+    ident = np.eye(nd + 1, dtype=np.float32)
+    if hr_moving:
+        case = synth.Case(mode, g, us, g, mr, [1.0] * nd, r, True, {}, ident)
+    else:
+        case = synth.Case(mode, g, mr, g, us, [1.0] * nd, r, False, {}, ident)
+    ctx = make_context(case)
+    assert ctx.evaluate(ident) == 0.0
+    assert oracle_eval(case, ident, use_boxsum=False) == 0.0
+    # sigma is not zero everywhere: the zero comes from the clipped measures
+    _, f = ctx.evaluate_fields(ident)
+    assert f["sigma"].max() > 0.0 and f["measure"].max() == 0.0
