@@ -274,3 +274,46 @@ def test_flat_mr_gives_zero(kind, hr_moving):
     # sigma is not zero everywhere: the zero comes from the clipped measures
     _, f = ctx.evaluate_fields(ident)
     assert f["sigma"].max() > 0.0 and f["measure"].max() == 0.0
+
+
+@pytest.mark.parametrize("hr_moving", [True, False])
+@pytest.mark.parametrize("kind", ["2d", "3d_r3"])
+def test_extreme_transforms_match_oracle(kind, hr_moving):
+    """Large rotations (about 30, 90 and 180 degrees), strong scaling (0.6x,
+    1.7x), shear and a translation that leaves part of the grid out of view:
+    the sampler's interior fast path must switch off exactly where samples
+    leave the moving image, and the values follow the oracle.
+
+    The angles sit off exact multiples of 90 degrees: there every sample
+    lands on an integer pixel and the border ones exactly on 0 or dim - 1,
+    where inside/outside flips on a 1e-7-voxel difference (the float32
+    matrix's cos 90 = -4.4e-8) -- below the sampler's FP32 resolution, so
+    the FP64 oracle and any FP32 evaluation, the reference's included, may
+    decide such ties differently."""
+    from lc2registration_gb300.geometry import affine2d, affine3d
+
+    case = _case(kind)
+    if not hr_moving:
+        case = _hr_fixed(case)
+    c = case.fixed_geom.center()
+    if case.mode == "2D":
+        mats = [affine2d(a, t, s, sh, c[:2], (0, 0)) for a, t, s, sh in
+                [(30.0, (2, -3), (1.0, 1.0), 0.0), (90.4, (0.3, 0), (1.0, 1.0), 0.0),
+                 (179.3, (1, 1), (1.0, 1.0), 0.0), (10.0, (0, 0), (0.6, 0.6), 0.0),
+                 (-15.0, (5, 0), (1.7, 1.2), 0.2), (5.0, (20, -15), (1.0, 1.0), 0.0)]]
+    else:
+        mats = [affine3d(rot, t, s, sh, c, (0, 0, 0)) for rot, t, s, sh in
+                [((30.0, 0, 0), (2, -3, 1), (1, 1, 1), (0, 0, 0)),
+                 ((0, 90.4, 0), (0.3, 0, 0), (1, 1, 1), (0, 0, 0)),
+                 ((0, 0, 179.3), (1, 1, 0), (1, 1, 1), (0, 0, 0)),
+                 ((10.0, -20.0, 15.0), (0, 0, 0), (0.6, 0.7, 0.6), (0.1, 0, -0.1)),
+                 ((5.0, 5.0, 5.0), (12, -10, 8), (1.7, 1.3, 1.0), (0, 0.2, 0))]]
+    mats = np.stack(mats).astype(np.float32)
+    ctx = make_context(case)
+    got = ctx.evaluate_batch(mats)
+    for k in range(len(mats)):
+        ref = oracle_eval(case, mats[k], use_boxsum=False)
+        if ref == 0.0:
+            assert got[k] == 0.0, k
+        else:
+            assert abs(got[k] / ref - 1.0) < REL_LC2, (k, got[k], ref)
