@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="default launch options")
+    ap.add_argument("--tile-rows", type=int, default=0,
+                    help="with --no-autotune: tile height of the fused 3D kernel (8, 16, 24; "
+                         "0 = the library's default)")
     ap.add_argument("--no-small", action="store_true", help="skip the 2D 256^2 / 3D 96^3 lines")
     ap.add_argument("--no-stack", action="store_true", help="skip the 2D-to-3D frame-stack line")
     ap.add_argument("--no-fixed", action="store_true",
@@ -506,7 +509,12 @@ def main():
                        case.hr_moving, args.storage, device=local)
     ctx.set_images(case.fixed, case.moving)
     # tile height, kernel variant, z-chunk; timed on 64 transforms
-    tuned = (16, 0) if args.no_autotune else ctx.autotune(mats[:64])
+    if args.no_autotune:
+        if args.tile_rows:
+            ctx.set_option(capi.OPTION_TILE_ROWS, args.tile_rows)
+        tuned = (args.tile_rows or 24, 0)
+    else:
+        tuned = ctx.autotune(mats[:64])
     K = mats.shape[0]
     stream = torch.cuda.ExternalStream(ctx.stream())
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")

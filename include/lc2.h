@@ -143,9 +143,12 @@ int lc2_warp_affine_2d(const float* src, int sw, int sh, float* dst, int dw, int
 long long lc2_launch_count(const lc2_context* ctx);
 
 /* Tuning options (lc2_set_option). LC2_OPTION_TILE_ROWS: output rows per
- * tile of the fused 3D kernel, 16 (one CTA per SM) or 8 (two per SM); 0 =
- * automatic. No counterpart in the reference (its block sizes are arguments
- * of CalculateGradient / GetSimilarityMetric, src/cu_LC2/cu_lc2_3d.cuh:36-41). */
+ * tile of the fused 3D kernel: 16 (one CTA per SM), 24 (one 768-thread CTA
+ * per SM; resampled MR/CT only, the resampled-ultrasound kernel takes it as
+ * 16) or 8 (two per SM); 0 = automatic (24 for patch radius 3 or 4 where it
+ * exists, else 16). No counterpart in the reference (its block sizes are
+ * arguments of CalculateGradient / GetSimilarityMetric,
+ * src/cu_LC2/cu_lc2_3d.cuh:36-41). */
 enum { LC2_OPTION_TILE_ROWS = 1 };
 /* LC2_OPTION_ZCHUNK: output slices each CTA of the fused 3D kernel marches
  * through (0 = automatic). LC2_OPTION_GRAPHS: 1 (default) replays

@@ -565,6 +565,16 @@ int launch_group_generic(lc2_context* c, int k0, int cnt, float* osig, float* om
                               cnt, osig, omeas);
 }
 
+// Output rows per tile of the fused kernels: the option if set, else 24 for
+// the 3D kernel of a resampled MR/CT with patch radius 3 or 4 (one 768-thread
+// CTA per SM: the fastest measured at 96^3 to 256^3, for one transform or
+// 512; at radius 2 16-row tiles were faster), else 16.
+int tile_rows(const lc2_context* c) {
+  if (c->tile_rows > 0) return c->tile_rows;
+  const int r = c->cfg.patch_size;
+  return (c->lc2_nd == 3 && c->cfg.high_res_is_moving && (r == 3 || r == 4)) ? 24 : 16;
+}
+
 // The fused kernel (static ultrasound): one launch for `cnt` transforms.
 int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
   c->acc_clean = false;
@@ -584,7 +594,7 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
   L.out_measure = omeas;
   L.nd = c->lc2_nd;
   L.wnd = c->warp_nd;
-  L.tile_height = c->tile_rows > 0 ? c->tile_rows : 16;
+  L.tile_height = tile_rows(c);
   // a slice's tiles index one grid dimension (<= 65535): 8-row tiles only
   // where they fit (16-row tiles always do, checked when the context is made)
   if (L.tile_height == 8 &&
@@ -628,7 +638,7 @@ int launch_fused_fixed(lc2_context* c, int k0, int cnt) {
   L.acc = c->d_acc;
   L.nd = c->lc2_nd;
   L.wnd = c->warp_nd;
-  L.tile_height = c->tile_rows > 0 ? c->tile_rows : 16;
+  L.tile_height = tile_rows(c);
   if (L.tile_height == 8 &&
       (long long)((c->virt.dim[0] + 31) / 32) * ((c->virt.dim[1] + 7) / 8) > 65535)
     L.tile_height = 16;
@@ -976,10 +986,10 @@ long long lc2_launch_count(const lc2_context* c) { return c ? c->launches : 0; }
 int lc2_set_option(lc2_context* c, int option, int value) {
   if (!c) return fail(LC2_ERR_INVALID_ARGUMENT, "null context");
   if (option == LC2_OPTION_TILE_ROWS) {
-    if (value != 0 && value != 8 && value != 16)
-      return fail(LC2_ERR_INVALID_ARGUMENT, "tile rows must be 0, 8 or 16");
-    if (value == 16 && c->lc2_nd == 3 && c->cfg.patch_size > 4)
-      return fail(LC2_ERR_UNSUPPORTED, "16-row tiles need a 3D patch radius <= 4");
+    if (value != 0 && value != 8 && value != 16 && value != 24)
+      return fail(LC2_ERR_INVALID_ARGUMENT, "tile rows must be 0, 8, 16 or 24");
+    if (value >= 16 && c->lc2_nd == 3 && c->cfg.patch_size > 4)
+      return fail(LC2_ERR_UNSUPPORTED, "%d-row tiles need a 3D patch radius <= 4", value);
     c->tile_rows = value;
     drop_graphs(c);
     return LC2_OK;
@@ -2114,7 +2124,10 @@ extern "C" int lc2_autotune(lc2_context* c, const float* matrices, int count, in
   const bool hrm = c->cfg.high_res_is_moving != 0;
   if (c->lc2_nd == 3 && !c->mi && !c->generic) {
     LC2_TRY(lc2_stage_transforms(c, matrices, count));
-    std::vector<int> rows = (r <= 4) ? std::vector<int>{16, 8} : std::vector<int>{8};
+    // 24-row tiles exist for the kernel of a resampled MR/CT only
+    std::vector<int> rows = (r > 4) ? std::vector<int>{8}
+                            : hrm   ? std::vector<int>{16, 24, 8}
+                                    : std::vector<int>{16, 8};
     const int vz = c->virt.dim[2];
     std::vector<int> chunks{0};
     for (int zc : {vz, vz / 2, vz / 4, 64, 32})
@@ -2178,7 +2191,7 @@ extern "C" int lc2_autotune(lc2_context* c, const float* matrices, int count, in
     }
     if (st != LC2_OK) return st;
   }
-  if (tile_rows) *tile_rows = c->tile_rows > 0 ? c->tile_rows : 16;
+  if (tile_rows) *tile_rows = ::tile_rows(c);
   if (zchunk) *zchunk = c->zchunk;
   return LC2_OK;
 }

@@ -47,6 +47,11 @@ struct FusedParams {
 
 constexpr int kLimbs = 12;
 
+// Rows of the band that fixes a 3D tile's sampling base: every tile height
+// (8, 16, 24) divides it, so a tile never straddles two bands and each voxel
+// is sampled from the same base whichever tile height computes it.
+constexpr int kBand = 48;
+
 // Compile-time geometry of one fused CTA: a 32 x TY output tile, patch radius R.
 template <int ND, int TY, int R>
 struct FusedGeom {
@@ -64,8 +69,11 @@ struct FusedGeom {
   static constexpr int WP = (NPW + NT - 1) / NT;    // resampled points per thread
   static constexpr int NPLANES = (ND == 3) ? 3 : 1;
   // leaving ring entries per point: qM, qG, and qU where shared memory allows
-  // (16-row tiles run one CTA per SM; 8-row tiles keep two CTAs resident)
-  static constexpr int RINGW = (ND == 3 && TY == 16) ? 3 : 2;
+  // and it pays: 16-row tiles (one CTA per SM) and 24-row tiles of radius 3
+  // (+10 % over reloading the leaving ultrasound; at radius 4 the halo leaves
+  // no room, at radius 2 it measured 1.5 % slower). 8-row tiles keep two CTAs
+  // resident.
+  static constexpr int RINGW = (ND == 3 && (TY == 16 || (TY == 24 && R == 3))) ? 3 : 2;
   // shared memory: M plane, interleaved (Sz, Dz) plane, leaving ring, limb planes
   static constexpr size_t OFF_LV = sizeof(float) * (size_t)NPLANES * NPW;
   static constexpr size_t OFF_A = OFF_LV + sizeof(int) * (size_t)RING * RINGW * NP;
@@ -515,8 +523,9 @@ __device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
   return acc_m;
 }
 
-// CTAs per SM each variant is compiled for: 2D tiles 4; 3D 16-row tiles 1;
-// 3D 8-row tiles 2 up to radius 4 (beyond, shared memory holds only one).
+// CTAs per SM each variant is compiled for: 2D tiles 4; 3D 16- and 24-row
+// tiles 1; 3D 8-row tiles 2 up to radius 4 (beyond, shared memory holds only
+// one).
 constexpr int fused_min_blocks(int nd, int ty, int r) {
   return nd == 2 ? 4 : (ty == 8 && r <= 4 ? 2 : 1);
 }
@@ -545,11 +554,11 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
   const int x0 = (tile % P.ntx) * 32, y0 = (tile / P.ntx) * TY;
   const Xform* X = xf + k0 + slot;
   const int gx0 = x0 - R - 1, gy0 = y0 - R - 1;  // origin of the resampled region
-  // Sampling base: (x0 - R - 1, 16 floor(y0 / 16) - R - 1). Tiles are 32
-  // wide in every kernel and 8 or 16 rows high, so this base -- and with it
-  // every sample, patch sum and LC2 value -- is the same whichever tile
+  // Sampling base: (x0 - R - 1, 48 floor(y0 / 48) - R - 1). Tiles are 32
+  // wide in every kernel and 8, 16 or 24 rows high, so this base -- and with
+  // it every sample, patch sum and LC2 value -- is the same whichever tile
   // height computes an output voxel. yb: row offset of the region origin.
-  const int yb = y0 & 15;
+  const int yb = y0 % kBand;
   const int ox = tid & 31, oy = tid >> 5;
   long long acc_m = 0;
 
@@ -841,14 +850,16 @@ cudaError_t fused_launch_rt(const FusedLaunch& L) {
   return cudaGetLastError();
 }
 
-// Tile heights: 3D patches of radius <= 4 run 32x16 tiles (one CTA per SM)
-// or 32x8 tiles (two per SM); larger radii only fit 32x8; 2D runs 32x16.
+// Tile heights: 3D patches of radius <= 4 run 32x16 tiles (one CTA per SM),
+// 32x24 tiles (one 768-thread CTA per SM) or 32x8 tiles (two per SM); larger
+// radii only fit 32x8; 2D runs 32x16.
 template <int ND, int WND, typename T, int R>
 cudaError_t fused_launch_r(const FusedLaunch& L) {
   if constexpr (ND == 3 && R > 4) {
     return fused_launch_rt<ND, WND, T, R, 8>(L);
   } else if constexpr (ND == 3) {
     if (L.tile_height == 8) return fused_launch_rt<ND, WND, T, R, 8>(L);
+    if (L.tile_height == 24) return fused_launch_rt<ND, WND, T, R, 24>(L);
     return fused_launch_rt<ND, WND, T, R, 16>(L);
   } else {
     return fused_launch_rt<ND, WND, T, R, 16>(L);

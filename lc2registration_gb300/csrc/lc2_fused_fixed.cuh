@@ -121,10 +121,10 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
   const int tile = blockIdx.y;
   const int x0 = (tile % P.ntx) * 32, y0 = (tile / P.ntx) * TY;
   const Xform* X = xf + k0 + slot;
-  // sampling base (x0 - R - 1, 16 floor(y0 / 16) - R - 1), as in k_fused, so
+  // sampling base (x0 - R - 1, 48 floor(y0 / 48) - R - 1), as in k_fused, so
   // 8- and 16-row tiles sample every voxel identically
   const int gx0 = x0 - R - 1, gy0 = y0 - R - 1;
-  const int yb = y0 & 15;
+  const int yb = y0 % kBand;
   const int ox = tid & 31, oy = tid >> 5;
   const int zb = blockIdx.z * P.zchunk;
   const int ze = min(zb + P.zchunk, P.vz);

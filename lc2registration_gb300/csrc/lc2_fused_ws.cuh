@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(WsGeom<R>::NT, 1)
   const int x0 = (tile % P.ntx) * 32, y0 = (tile / P.ntx) * TY;
   const Xform* X = xf + k0 + slot;
   const int gx0 = x0 - R - 1, gy0 = y0 - R - 1;
-  const int yb = y0 & 15;  // 0: tiles are 16 rows high
+  const int yb = y0 % kBand;  // the sampling base of k_fused
   const int zb = blockIdx.z * P.zchunk;
   const int ze = min(zb + P.zchunk, P.vz);
   const int e0 = zb - R;                 // first slice entering the window

@@ -41,7 +41,7 @@ def test_zchunk_and_tile_rows_do_not_change_results(case3d):
     ctx = make_context(case3d)
     mats = perturbed(case3d, np.random.default_rng(1), 6)
     ref = ctx.evaluate_batch(mats)
-    for rows in (8, 16):
+    for rows in (8, 16, 24):
         ctx.set_option(capi.OPTION_TILE_ROWS, rows)
         for zc in (0, 6, 7, 13, 40, 1000):
             ctx.set_option(capi.OPTION_ZCHUNK, zc)
@@ -53,15 +53,16 @@ def test_autotune_keeps_results(case3d):
     mats = perturbed(case3d, np.random.default_rng(2), 16)
     ref = ctx.evaluate_batch(mats)
     rows, zc = ctx.autotune(mats)
-    assert rows in (8, 16) and zc >= 0
+    assert rows in (8, 16, 24) and zc >= 0
     np.testing.assert_array_equal(ctx.evaluate_batch(mats), ref)
 
 
 def test_tile_rows_16_rejected_for_large_3d_radius():
     case = synth.case_3d(seed=22, mr_size=40, us_size=32, r=5, blobs=4)
     ctx = make_context(case)
-    with pytest.raises(capi.LC2Error, match="UNSUPPORTED"):
-        ctx.set_option(capi.OPTION_TILE_ROWS, 16)
+    for rows in (16, 24):
+        with pytest.raises(capi.LC2Error, match="UNSUPPORTED"):
+            ctx.set_option(capi.OPTION_TILE_ROWS, rows)
     rows, _ = ctx.autotune(perturbed(case, np.random.default_rng(3), 2))
     assert rows == 8
 
@@ -96,3 +97,35 @@ def test_stream_priority_keeps_results(case3d):
     ctx.set_option(capi.OPTION_STREAM_PRIORITY, -1000)
     np.testing.assert_array_equal(ctx.evaluate_batch(mats), ref)
     np.testing.assert_array_equal(_staged(ctx, mats), ref)
+
+
+def test_tile_heights_agree_across_sampling_bands():
+    """A virtual grid 110 rows high spans three 48-row sampling bands (the
+    rows that fix a tile's sampling base): 8-, 16- and 24-row tiles, whose
+    tiles start at different offsets inside a band, give the same bits, and
+    the LC2 values match the oracle."""
+    from lc2registration_gb300.geometry import Geometry, affine3d
+    from tests.helpers import oracle_eval
+    from tests.test_gpu_parity import REL_LC2
+
+    mg = Geometry((64, 128, 24), (1.0, 1.0, 1.0), (0.0, 0.0, 0.0))
+    mr = synth.mr_phantom((24, 128, 64), 8, 1.5, seed=33)
+    ug = Geometry((40, 110, 12), (1.0, 1.0, 1.0), (12.0, 9.0, 6.0))
+    p = dict(rot=[2.0, -3.0, 4.0], trans=[1.5, -2.0, 0.5], scale=[1.02, 0.98, 1.0],
+             shear=[0.01, 0.0, -0.01])
+    mat = affine3d(p["rot"], p["trans"], p["scale"], p["shear"], ug.center(), (0.0, 0.0, 0.0))
+    us = synth.us_from_mr(mr, mg, ug, mat, 33)
+    case = synth.Case("3D", ug, us, mg, mr, [1.0, 1.0, 1.0], 4, True, p, mat.astype(np.float32))
+    mats = np.concatenate([case.true_mat[None], perturbed(case, np.random.default_rng(4), 3)])
+    ctx = make_context(case)
+    ref = None
+    for rows in (24, 16, 8):
+        ctx.set_option(capi.OPTION_TILE_ROWS, rows)
+        got = ctx.evaluate_batch(mats)
+        if ref is None:
+            ref = got
+        np.testing.assert_array_equal(got, ref)
+    for k in range(len(mats)):
+        want = oracle_eval(case, mats[k], use_boxsum=False)
+        assert want > 0.01
+        assert abs(ref[k] / want - 1.0) < REL_LC2, (k, ref[k], want)
