@@ -64,20 +64,23 @@ struct FusedGeom {
   static constexpr int HXP = (((HX + 3) / 4) | 1) * 4, TXP = 33;
   static constexpr int W = 2 * R + 1;
   static constexpr int NP = HX * HY, NPW = PW * PH;
-  static constexpr int RING = (ND == 3) ? 2 * R + 2 : 0;
+  // quantised-field ring of the z window: 2R+1 slices, the entering slice
+  // taking the leaving slice's slot (each entry is read, then rewritten, by
+  // the one thread that owns its halo point)
+  static constexpr int RING = (ND == 3) ? 2 * R + 1 : 0;
   static constexpr int MAXP = (NP + NT - 1) / NT;   // halo points per thread
   static constexpr int WP = (NPW + NT - 1) / NT;    // resampled points per thread
   static constexpr int NPLANES = (ND == 3) ? 3 : 1;
   // leaving ring entries per point: qM, qG, and qU where shared memory allows
-  // and it pays: 16-row tiles (one CTA per SM) and 24-row tiles of radius 3
-  // (+10 % over reloading the leaving ultrasound; at radius 4 the halo leaves
-  // no room, at radius 2 it measured 1.5 % slower). 8-row tiles keep two CTAs
-  // resident.
-  static constexpr int RINGW = (ND == 3 && (TY == 16 || (TY == 24 && R == 3))) ? 3 : 2;
+  // (16- and 24-row tiles, one CTA per SM); 8-row tiles keep two CTAs
+  // resident and reload the leaving ultrasound instead
+  static constexpr int RINGW = (ND == 3 && (TY == 16 || TY == 24)) ? 3 : 2;
   // shared memory: M plane, interleaved (Sz, Dz) plane, leaving ring, limb planes
   static constexpr size_t OFF_LV = sizeof(float) * (size_t)NPLANES * NPW;
   static constexpr size_t OFF_A = OFF_LV + sizeof(int) * (size_t)RING * RINGW * NP;
   static constexpr size_t BYTES = OFF_A + sizeof(int) * (size_t)kLimbs * HY * HXP;
+  static_assert(ND == 2 || TY == 8 || BYTES + 1024 <= 227 * 1024,
+                "one CTA's shared memory must fit an SM");
 };
 
 // Halo point q of a 2D tile -> (hy, hx): the first 32 columns row by row,
@@ -733,16 +736,8 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
           const float m = mc[pc[j]];
           const float g = fused_sobel_sd<G::PW>(SD, pc[j]);
           const int qm = quant(m, P.qm), qg = quant(g, P.qg), qu = quant(u_in[j], P.qu);
-          lv_in[p] = qm;
-          lv_in[G::NP + p] = qg;
-          if constexpr (G::RINGW == 3) lv_in[2 * G::NP + p] = qu;
-          accp[j][0] += (long long)qu * qm;
-          accp[j][1] += (long long)qu * qg;
-          accp[j][2] += (long long)qm * qm;
-          accp[j][3] += (long long)qg * qg;
-          accp[j][4] += (long long)qm * qg;
-          accq[j][0] += qm;
-          accq[j][1] += qg;
+          // the leaving slice's ring slot is the entering slice's: read it
+          // before it is overwritten (only this thread touches entry p)
           if (leave) {
             const int qul = (G::RINGW == 3) ? lv_out[2 * G::NP + p] : quant(u_out[j], P.qu);
             const int qml = lv_out[p], qgl = lv_out[G::NP + p];
@@ -754,6 +749,16 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
             accq[j][0] -= qml;
             accq[j][1] -= qgl;
           }
+          lv_in[p] = qm;
+          lv_in[G::NP + p] = qg;
+          if constexpr (G::RINGW == 3) lv_in[2 * G::NP + p] = qu;
+          accp[j][0] += (long long)qu * qm;
+          accp[j][1] += (long long)qu * qg;
+          accp[j][2] += (long long)qm * qm;
+          accp[j][3] += (long long)qg * qg;
+          accp[j][4] += (long long)qm * qg;
+          accq[j][0] += qm;
+          accq[j][1] += qg;
           if (out) {
             // the same limb layout as fused_limbs: qM, qG, then (lo, hi) per product
             int* a = A + pa_off[j];

@@ -236,11 +236,13 @@ __global__ void __launch_bounds__(WsGeom<R>::NT, 1)
         const int qm = quant(m, P.qm), qg = quant(g, P.qg);
         int Li[kLimbs];
         fused_limbs(quant(u, P.qu), qm, qg, P.kbits, Li);
+        // the leaving slice's ring slot is the entering slice's: read first
+        const int qml = leave ? lv_out[p] : 0, qgl = leave ? lv_out[G::NP + p] : 0;
         lv_in[p] = qm;
         lv_in[G::NP + p] = qg;
         if (leave) {
           int Lo[kLimbs];
-          fused_limbs(quant(ul, P.qu), lv_out[p], lv_out[G::NP + p], P.kbits, Lo);
+          fused_limbs(quant(ul, P.qu), qml, qgl, P.kbits, Lo);
 #pragma unroll
           for (int k = 0; k < kLimbs; ++k) acc32[j][k] += Li[k] - Lo[k];
         } else {
