@@ -99,11 +99,12 @@ def test_stream_priority_keeps_results(case3d):
     np.testing.assert_array_equal(_staged(ctx, mats), ref)
 
 
-def test_tile_heights_agree_across_sampling_bands():
+@pytest.mark.parametrize("r", [1, 2, 3, 4])
+def test_tile_heights_agree_across_sampling_bands(r):
     """A virtual grid 110 rows high spans three 48-row sampling bands (the
     rows that fix a tile's sampling base): 8-, 16- and 24-row tiles, whose
     tiles start at different offsets inside a band, give the same bits, and
-    the LC2 values match the oracle."""
+    the LC2 values match the oracle, at every radius with 24-row tiles."""
     from lc2registration_gb300.geometry import Geometry, affine3d
     from tests.helpers import oracle_eval
     from tests.test_gpu_parity import REL_LC2
@@ -115,7 +116,7 @@ def test_tile_heights_agree_across_sampling_bands():
              shear=[0.01, 0.0, -0.01])
     mat = affine3d(p["rot"], p["trans"], p["scale"], p["shear"], ug.center(), (0.0, 0.0, 0.0))
     us = synth.us_from_mr(mr, mg, ug, mat, 33)
-    case = synth.Case("3D", ug, us, mg, mr, [1.0, 1.0, 1.0], 4, True, p, mat.astype(np.float32))
+    case = synth.Case("3D", ug, us, mg, mr, [1.0, 1.0, 1.0], r, True, p, mat.astype(np.float32))
     mats = np.concatenate([case.true_mat[None], perturbed(case, np.random.default_rng(4), 3)])
     ctx = make_context(case)
     ref = None
