@@ -146,9 +146,12 @@ long long lc2_launch_count(const lc2_context* ctx);
  * tile of the fused 3D kernel: 16 (one CTA per SM), 24 (one 768-thread CTA
  * per SM; resampled MR/CT only, the resampled-ultrasound kernel takes it as
  * 16) or 8 (two per SM); 0 = automatic (24 for patch radius 3 or 4 where it
- * exists, else 16). No counterpart in the reference (its block sizes are
- * arguments of CalculateGradient / GetSimilarityMetric,
- * src/cu_LC2/cu_lc2_3d.cuh:36-41). */
+ * exists, else 16). 2D and 2D-to-3D contexts with a resampled MR/CT: 16 or
+ * 32 (two 1024-thread CTAs per SM, patch radius 4 to 6; other radii take
+ * it as 16); 0 = per launch (32 where it exists and the launch has four
+ * CTAs per SM or more). No counterpart in the
+ * reference (its block sizes are arguments of CalculateGradient /
+ * GetSimilarityMetric, src/cu_LC2/cu_lc2_3d.cuh:36-41). */
 enum { LC2_OPTION_TILE_ROWS = 1 };
 /* LC2_OPTION_ZCHUNK: output slices each CTA of the fused 3D kernel marches
  * through (0 = automatic). LC2_OPTION_GRAPHS: 1 (default) replays

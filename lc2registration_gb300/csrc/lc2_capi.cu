@@ -568,9 +568,10 @@ int launch_group_generic(lc2_context* c, int k0, int cnt, float* osig, float* om
 // Output rows per tile of the fused kernels: the option if set, else 24 for
 // the 3D kernel of a resampled MR/CT with patch radius 3 or 4 (one 768-thread
 // CTA per SM: the fastest measured at 96^3 to 256^3, for one transform or
-// 512; at radius 2 16-row tiles were faster), else 16.
+// 512; at radius 2 16-row tiles were faster), 0 (per launch) in 2D, else 16.
 int tile_rows(const lc2_context* c) {
   if (c->tile_rows > 0) return c->tile_rows;
+  if (c->lc2_nd == 2) return 0;  // chosen per launch: 32 rows for large launches, else 16
   const int r = c->cfg.patch_size;
   return (c->lc2_nd == 3 && c->cfg.high_res_is_moving && (r == 3 || r == 4)) ? 24 : 16;
 }
@@ -986,8 +987,10 @@ long long lc2_launch_count(const lc2_context* c) { return c ? c->launches : 0; }
 int lc2_set_option(lc2_context* c, int option, int value) {
   if (!c) return fail(LC2_ERR_INVALID_ARGUMENT, "null context");
   if (option == LC2_OPTION_TILE_ROWS) {
-    if (value != 0 && value != 8 && value != 16 && value != 24)
-      return fail(LC2_ERR_INVALID_ARGUMENT, "tile rows must be 0, 8, 16 or 24");
+    if (value != 0 && value != 8 && value != 16 && value != 24 && value != 32)
+      return fail(LC2_ERR_INVALID_ARGUMENT, "tile rows must be 0, 8, 16, 24 or 32");
+    if (value == 32 && c->lc2_nd == 3)
+      return fail(LC2_ERR_UNSUPPORTED, "32-row tiles exist for 2D and 2D-to-3D contexts only");
     if (value >= 16 && c->lc2_nd == 3 && c->cfg.patch_size > 4)
       return fail(LC2_ERR_UNSUPPORTED, "%d-row tiles need a 3D patch radius <= 4", value);
     c->tile_rows = value;

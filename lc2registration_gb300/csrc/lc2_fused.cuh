@@ -463,19 +463,23 @@ __device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
   const int ntx = P.ntx;
   const int x0 = (tile % ntx) * 32, y0 = (tile / ntx) * TY;
   const int gx0 = x0 - R - 1, gy0 = y0 - R - 1;
+  // sampling base (x0 - R - 1, 32 floor(y0 / 32) - R - 1): tiles are 16 or
+  // 32 rows high, and both heights sample every pixel identically
+  const int yb = y0 & 31;
   if (tid == 0) {
 #pragma unroll
     for (int i = 0; i < 9; ++i) T.A[i] = X->ah[i];
-    T.inside = region_base<WND, G::PW, G::PH>(*X, T.A, P, gx0, gy0, 0, 0, true, T.ib, T.fb) ? 1 : 0;
+    T.inside =
+        region_base<WND, G::PW, G::PH>(*X, T.A, P, gx0, gy0, yb, 0, true, T.ib, T.fb) ? 1 : 0;
   }
   __syncthreads();
   if (T.inside) {
     for (int i = tid; i < G::NPW; i += NT) {
       const int py = i / G::PW, px = i - py * G::PW;
       if constexpr (WND == 3)
-        mc[i] = fused_sample_inside<TM>(mov, P, T.A, T.ib, T.fb, px, py);
+        mc[i] = fused_sample_inside<TM>(mov, P, T.A, T.ib, T.fb, px, py + yb);
       else
-        mc[i] = fused_sample_inside2<TM>(mov, P, T.A, T.ib, T.fb, px, py);
+        mc[i] = fused_sample_inside2<TM>(mov, P, T.A, T.ib, T.fb, px, py + yb);
     }
   } else {
     for (int i = tid; i < G::NPW; i += NT) {
@@ -483,7 +487,7 @@ __device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
       const int gx = gx0 + px, gy = gy0 + py;
       float v = 0.0f;
       if (gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy)
-        v = fused_sample<WND, TM>(mov, P, T.A, T.ib, T.fb, px, py);
+        v = fused_sample<WND, TM>(mov, P, T.A, T.ib, T.fb, px, py + yb);
       mc[i] = v;
     }
   }
@@ -526,11 +530,11 @@ __device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
   return acc_m;
 }
 
-// CTAs per SM each variant is compiled for: 2D tiles 4; 3D 16- and 24-row
-// tiles 1; 3D 8-row tiles 2 up to radius 4 (beyond, shared memory holds only
-// one).
+// CTAs per SM each variant is compiled for: 2D 16-row tiles 4, 32-row tiles
+// 2; 3D 16- and 24-row tiles 1; 3D 8-row tiles 2 up to radius 4 (beyond,
+// shared memory holds only one).
 constexpr int fused_min_blocks(int nd, int ty, int r) {
-  return nd == 2 ? 4 : (ty == 8 && r <= 4 ? 2 : 1);
+  return nd == 2 ? (ty == 32 ? 2 : 4) : (ty == 8 && r <= 4 ? 2 : 1);
 }
 
 template <int ND, int WND, typename TM, typename TS, int TY, int R>
@@ -857,7 +861,8 @@ cudaError_t fused_launch_rt(const FusedLaunch& L) {
 
 // Tile heights: 3D patches of radius <= 4 run 32x16 tiles (one CTA per SM),
 // 32x24 tiles (one 768-thread CTA per SM) or 32x8 tiles (two per SM); larger
-// radii only fit 32x8; 2D runs 32x16.
+// radii only fit 32x8; 2D runs 32x32 (two 1024-thread CTAs per SM, radius
+// <= 6) or 32x16 tiles (four per SM).
 template <int ND, int WND, typename T, int R>
 cudaError_t fused_launch_r(const FusedLaunch& L) {
   if constexpr (ND == 3 && R > 4) {
@@ -865,6 +870,14 @@ cudaError_t fused_launch_r(const FusedLaunch& L) {
   } else if constexpr (ND == 3) {
     if (L.tile_height == 8) return fused_launch_rt<ND, WND, T, R, 8>(L);
     if (L.tile_height == 24) return fused_launch_rt<ND, WND, T, R, 24>(L);
+    return fused_launch_rt<ND, WND, T, R, 16>(L);
+  } else if constexpr (R >= 4 && R <= 6) {
+    // 32-row tiles (two 1024-thread CTAs per SM, a smaller halo per pixel)
+    // where the launch has CTAs enough for the GPU: two per SM, twice over
+    if (L.tile_height == 32 ||
+        (L.tile_height != 16 && (long long)L.cnt * ((L.P.vx + 31) / 32) * ((L.P.vy + 31) / 32) >=
+                                    4LL * L.sms))
+      return fused_launch_rt<ND, WND, T, R, 32>(L);
     return fused_launch_rt<ND, WND, T, R, 16>(L);
   } else {
     return fused_launch_rt<ND, WND, T, R, 16>(L);

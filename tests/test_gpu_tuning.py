@@ -74,7 +74,10 @@ def test_2d_context_graphs():
     got = ctx.evaluate_batch(mats)
     np.testing.assert_array_equal(got, _staged(ctx, mats))
     np.testing.assert_array_equal([ctx.evaluate(m) for m in mats], got)
-    assert ctx.autotune(mats) == (16, 0)
+    assert ctx.autotune(mats) == (0, 0)  # 2D: tile height chosen per launch
+    for rows in (16, 32, 0):
+        ctx.set_option(capi.OPTION_TILE_ROWS, rows)
+        np.testing.assert_array_equal(ctx.evaluate_batch(mats), got)
 
 
 @pytest.mark.parametrize("r", [1, 2, 4])
@@ -126,6 +129,35 @@ def test_tile_heights_agree_across_sampling_bands(r):
         if ref is None:
             ref = got
         np.testing.assert_array_equal(got, ref)
+    for k in range(len(mats)):
+        want = oracle_eval(case, mats[k], use_boxsum=False)
+        assert want > 0.01
+        assert abs(ref[k] / want - 1.0) < REL_LC2, (k, ref[k], want)
+
+
+@pytest.mark.parametrize("kind", ["2d_r5", "2dto3d_r4"])
+def test_2d_tile_heights_agree_and_match_oracle(kind):
+    """2D and 2D-to-3D contexts of radius 4-6 run 32-row tiles on large
+    launches and 16-row tiles on small ones; both sample from the same
+    32-row band, so the choice never changes a bit, and LC2 matches the
+    oracle."""
+    from lc2registration_gb300.geometry import Geometry
+    from tests.helpers import oracle_eval
+    from tests.test_gpu_parity import REL_LC2
+
+    if kind == "2d_r5":
+        case = synth.case_2d(seed=14, size=100, r=5)
+    else:
+        mr = synth.mr_phantom((40, 40, 40), 6, 1.5, seed=34)
+        mg = Geometry((40, 40, 40), (1, 1, 1), (0, 0, 0))
+        case = synth.frame_stack(mr, mg, 1, seed=35, sides=(70,), spacing=0.5, r=4)[0]
+    mats = np.concatenate([case.true_mat[None], perturbed(case, np.random.default_rng(6), 3)])
+    ctx = make_context(case)
+    ref = ctx.evaluate_batch(mats)
+    for rows in (32, 16, 0):
+        ctx.set_option(capi.OPTION_TILE_ROWS, rows)
+        np.testing.assert_array_equal(ctx.evaluate_batch(mats), ref)
+        np.testing.assert_array_equal([ctx.evaluate(m) for m in mats[:2]], ref[:2])
     for k in range(len(mats)):
         want = oracle_eval(case, mats[k], use_boxsum=False)
         assert want > 0.01
