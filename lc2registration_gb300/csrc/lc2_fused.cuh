@@ -47,6 +47,26 @@ struct FusedParams {
 
 constexpr int kLimbs = 12;
 
+// Patch voxels (2R+1)^ND and the limb split K of a patch of that size: the
+// largest K with (n + 1) 2^K <= 2^30, so every low limb's window sum stays
+// below 2^30 -- the rule by which the host sets FusedParams::kbits. The
+// kernels take both from their template radius, so multiplications by n and
+// the limb shifts and masks are immediates; the launchers check that the
+// host's kbits agrees.
+constexpr long long patch_voxels(int nd, int r) {
+  return (long long)(2 * r + 1) * (2 * r + 1) * (nd == 3 ? (2 * r + 1) : 1);
+}
+constexpr int limb_bits(long long n) {
+  int k = 0;
+  while (((n + 1) << (k + 1)) <= (1LL << 30)) ++k;
+  return k;
+}
+template <int ND, int R>
+struct PatchConst {
+  static constexpr long long N = patch_voxels(ND, R);
+  static constexpr int K = limb_bits(N);
+};
+
 // Rows of the band that fixes a 3D tile's sampling base: every tile height
 // (8, 16, 24) divides it, so a tile never straddles two bands and each voxel
 // is sampled from the same base whichever tile height computes it.
@@ -288,10 +308,10 @@ __device__ __forceinline__ void fused_xy(int* __restrict__ A) {
 
 // Clipped measure of one voxel from exact sums; sigma > 0 is the
 // precomputed weighting factor (0 marks an invalid patch).
-__device__ __forceinline__ float fused_solve(const FusedParams& P, float sigma, int s_u, int s_m,
-                                             int s_g, long long s_um, long long s_ug,
-                                             long long s_mm, long long s_gg, long long s_mg) {
-  const long long n = P.n;
+__device__ __forceinline__ float fused_solve(const FusedParams& P, long long n, float sigma,
+                                             int s_u, int s_m, int s_g, long long s_um,
+                                             long long s_ug, long long s_mm, long long s_gg,
+                                             long long s_mg) {
   long long d_mm = n * s_mm - (long long)s_m * s_m;
   long long d_gg = n * s_gg - (long long)s_g * s_g;
   long long d_mg = n * s_mg - (long long)s_m * s_g;
@@ -332,14 +352,17 @@ __device__ __forceinline__ float fused_solve(const FusedParams& P, float sigma, 
   return m;
 }
 
-// Patch sums from the 12 limbs of an output voxel, then its clipped measure.
+// Patch sums from the 12 limbs of an output voxel (patch of PatchConst<ND,R>
+// voxels), then its clipped measure.
+template <int ND, int R>
 __device__ __forceinline__ float fused_measure(const FusedParams& P, float sg, int s_u,
                                                const int* L) {
+  using C = PatchConst<ND, R>;
   long long Sx[5];
 #pragma unroll
   for (int i = 0; i < 5; ++i)
-    Sx[i] = (long long)L[3 + 2 * i] * (1LL << P.kbits) + (long long)L[2 + 2 * i];
-  return fused_solve(P, sg, s_u, L[0], L[1], Sx[0], Sx[1], Sx[2], Sx[3], Sx[4]);
+    Sx[i] = (long long)L[3 + 2 * i] * (1LL << C::K) + (long long)L[2 + 2 * i];
+  return fused_solve(P, C::N, sg, s_u, L[0], L[1], Sx[0], Sx[1], Sx[2], Sx[3], Sx[4]);
 }
 
 // Square root of a Sobel magnitude: PTX sqrt.approx (one instruction, a
@@ -502,7 +525,7 @@ __device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
     float u = 0.0f;
     if (gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy) u = ldf(Ust, (size_t)gy * P.vx + gx);
     int L[kLimbs];
-    fused_limbs(quant(u, P.qu), quant(m, P.qm), quant(g, P.qg), P.kbits, L);
+    fused_limbs(quant(u, P.qu), quant(m, P.qm), quant(g, P.qg), PatchConst<2, R>::K, L);
     int* a = A + hy * G::HXP + hx;
 #pragma unroll
     for (int k = 0; k < kLimbs; ++k) a[k * PA] = L[k];
@@ -522,7 +545,7 @@ __device__ __forceinline__ long long fused_tile_2d(const TM* __restrict__ mov,
       int L[kLimbs];
 #pragma unroll
       for (int k = 0; k < kLimbs; ++k) L[k] = a[k * PA];
-      m = fused_measure(P, sg, sv, L);
+      m = fused_measure<2, R>(P, sg, sv, L);
       acc_m = __float2int_rn(m * P.sum_scale);
     }
     if (out_measure) out_measure[gi] = m;
@@ -596,7 +619,7 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
         int L[kLimbs];
 #pragma unroll
         for (int k = 0; k < kLimbs; ++k) L[k] = a[k * PA];
-        m = fused_measure(P, sg, sv, L);
+        m = fused_measure<ND, R>(P, sg, sv, L);
         acc_m += __float2int_rn(m * P.sum_scale);
       }
       if (out_measure && slot == 0) out_measure[gi] = m;
@@ -622,7 +645,8 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
 #pragma unroll
       for (int k = 0; k < 5; ++k) accp[j][k] = 0;
     }
-    const unsigned long long kmask = (1ull << P.kbits) - 1ull;
+    constexpr int KB = PatchConst<ND, R>::K;
+    constexpr unsigned long long kmask = (1ull << KB) - 1ull;
     // per-thread constants of its halo points: plane index, A offset, U offset
     int pc[MAXP], pa_off[MAXP], pu[MAXP];
     bool pin[MAXP];
@@ -771,7 +795,7 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
 #pragma unroll
             for (int k = 0; k < 5; ++k) {
               a[(2 + 2 * k) * PA] = (int)((unsigned long long)accp[j][k] & kmask);
-              a[(3 + 2 * k) * PA] = (int)(accp[j][k] >> P.kbits);
+              a[(3 + 2 * k) * PA] = (int)(accp[j][k] >> KB);
             }
           }
         }
@@ -835,6 +859,8 @@ struct FusedLaunch {
 template <int ND, int WND, typename T, int R, int TY>
 cudaError_t fused_launch_rt(const FusedLaunch& L) {
   using G = FusedGeom<ND, TY, R>;
+  if (L.P.kbits != PatchConst<ND, R>::K || L.P.n != PatchConst<ND, R>::N)
+    return cudaErrorInvalidValue;
   auto kern = k_fused<ND, WND, T, T, TY, R>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)G::BYTES);

@@ -66,18 +66,20 @@ __device__ __forceinline__ void fixed_limbs(int* a, size_t pa, int su, int si, l
 
 // Sigma and measure of output voxel gi from its patch sums (limb stride ls)
 // and the static fields; adds both to the exact sums.
+template <int ND, int R>
 __device__ __forceinline__ void fixed_solve(const FusedParams& P, const FixedStatic& S,
                                             const int* a, int ls, size_t gi, long long& acc_m,
                                             long long& acc_s) {
   if (a[ls] != 0) return;  // a patch value <= 1e-6: sigma = 0
   const int su = a[0];
-  const long long uu = (long long)a[3 * ls] * (1LL << P.kbits) + a[2 * ls];
-  const long long um = (long long)a[5 * ls] * (1LL << P.kbits) + a[4 * ls];
-  const long long ug = (long long)a[7 * ls] * (1LL << P.kbits) + a[6 * ls];
+  constexpr int K = PatchConst<ND, R>::K;
+  const long long uu = (long long)a[3 * ls] * (1LL << K) + a[2 * ls];
+  const long long um = (long long)a[5 * ls] * (1LL << K) + a[4 * ls];
+  const long long ug = (long long)a[7 * ls] * (1LL << K) + a[6 * ls];
   const int sm = __ldg(S.s + gi), sg = __ldg(S.s + S.nv + gi);
   const long long dmm = __ldg(S.d + gi), dgg = __ldg(S.d + S.nv + gi),
                   dmg = __ldg(S.d + 2 * S.nv + gi);
-  const long long n = P.n;
+  constexpr long long n = PatchConst<ND, R>::N;
   float sigma, m;
   solve_centred(n * uu - (long long)su * su, dmm, dgg, dmg, n * um - (long long)su * sm,
                 n * ug - (long long)su * sg, P.thr_var, P.thr_m, P.thr_g, P.sig_scale, sigma, m);
@@ -183,10 +185,11 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
     constexpr int ls = TY * 32;
     if (x < P.vx && y < P.vy && a[ls] == 0) {
       const int su = a[0];
-      const long long uu = (long long)a[3 * ls] * (1LL << P.kbits) + a[2 * ls];
-      const long long um = (long long)a[5 * ls] * (1LL << P.kbits) + a[4 * ls];
-      const long long ug = (long long)a[7 * ls] * (1LL << P.kbits) + a[6 * ls];
-      const long long n = P.n;
+      constexpr int K = PatchConst<3, R>::K;
+      const long long uu = (long long)a[3 * ls] * (1LL << K) + a[2 * ls];
+      const long long um = (long long)a[5 * ls] * (1LL << K) + a[4 * ls];
+      const long long ug = (long long)a[7 * ls] * (1LL << K) + a[6 * ls];
+      constexpr long long n = PatchConst<3, R>::N;
       float sigma, m;
       solve_centred(n * uu - (long long)su * su, ndmm, ndgg, ndmg, n * um - (long long)su * nsm,
                     n * ug - (long long)su * nsg, P.thr_var, P.thr_m, P.thr_g, P.sig_scale, sigma, m);
@@ -256,7 +259,9 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
           sUM[j] -= (long long)qul * qml;
           sUG[j] -= (long long)qul * qgl;
         }
-        if (out) fixed_limbs(A + pa_off[j], PA, sU[j], sI[j], sUU[j], sUM[j], sUG[j], P.kbits);
+        if (out)
+          fixed_limbs(A + pa_off[j], PA, sU[j], sI[j], sUU[j], sUM[j], sUG[j],
+                      PatchConst<3, R>::K);
       }
     }
     {
@@ -332,7 +337,7 @@ __global__ void __launch_bounds__(512, 3)
     }
     const int qu = quant(u, P.qu);
     fixed_limbs(A + hy * G::HXP + hx, PA, qu, (u > 1e-6f) ? 0 : 1, (long long)qu * qu,
-                (long long)qu * qm, (long long)qu * qg, P.kbits);
+                (long long)qu * qm, (long long)qu * qg, PatchConst<2, R>::K);
   }
   __syncthreads();
   fused_xy<2, TY, R, 0, NL>(A);
@@ -340,7 +345,8 @@ __global__ void __launch_bounds__(512, 3)
   const int ox = tid & 31, oy = tid >> 5;
   const int x = x0 + ox, y = y0 + oy;
   if (x < P.vx && y < P.vy)
-    fixed_solve(P, S, A + oy * G::HXP + ox, (int)PA, (size_t)y * P.vx + x, acc_m, acc_s);
+    fixed_solve<2, R>(P, S, A + oy * G::HXP + ox, (int)PA, (size_t)y * P.vx + x, acc_m,
+                      acc_s);
   fixed_flush(acc_m, acc_s, acc + 2 * (size_t)(k0 + slot));
 }
 
@@ -361,6 +367,8 @@ struct FixedLaunch {
 template <typename T, int R, int TY>
 cudaError_t fixed_launch3(const FixedLaunch& L) {
   using F = FixedGeom<3, TY, R>;
+  if (L.P.kbits != PatchConst<3, R>::K || L.P.n != PatchConst<3, R>::N)
+    return cudaErrorInvalidValue;
   auto kern = k_fused_fixed3<T, TY, R>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)F::BYTES);
@@ -382,6 +390,8 @@ cudaError_t fixed_launch3(const FixedLaunch& L) {
 template <typename T, int R>
 cudaError_t fixed_launch2(const FixedLaunch& L) {
   using F = FixedGeom<2, 16, R>;
+  if (L.P.kbits != PatchConst<2, R>::K || L.P.n != PatchConst<2, R>::N)
+    return cudaErrorInvalidValue;
   FusedParams P = L.P;
   P.ntx = (P.vx + 31) / 32;
   const int nty = (P.vy + 15) / 16;

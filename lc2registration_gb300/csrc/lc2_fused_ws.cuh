@@ -235,14 +235,14 @@ __global__ void __launch_bounds__(WsGeom<R>::NT, 1)
         const float g = fused_sobel_sd<G::PW>(SD, pc[j]);
         const int qm = quant(m, P.qm), qg = quant(g, P.qg);
         int Li[kLimbs];
-        fused_limbs(quant(u, P.qu), qm, qg, P.kbits, Li);
+        fused_limbs(quant(u, P.qu), qm, qg, PatchConst<3, R>::K, Li);
         // the leaving slice's ring slot is the entering slice's: read first
         const int qml = leave ? lv_out[p] : 0, qgl = leave ? lv_out[G::NP + p] : 0;
         lv_in[p] = qm;
         lv_in[G::NP + p] = qg;
         if (leave) {
           int Lo[kLimbs];
-          fused_limbs(quant(ul, P.qu), qml, qgl, P.kbits, Lo);
+          fused_limbs(quant(ul, P.qu), qml, qgl, PatchConst<3, R>::K, Lo);
 #pragma unroll
           for (int k = 0; k < kLimbs; ++k) acc32[j][k] += Li[k] - Lo[k];
         } else {
@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(WsGeom<R>::NT, 1)
         int L[kLimbs];
 #pragma unroll
         for (int k = 0; k < kLimbs; ++k) L[k] = a[k * PA];
-        const float m = fused_measure(P, sg, sv, L);
+        const float m = fused_measure<3, R>(P, sg, sv, L);
         acc_m += __float2int_rn(m * P.sum_scale);
       }
     }
@@ -280,6 +280,8 @@ __global__ void __launch_bounds__(WsGeom<R>::NT, 1)
 template <typename T, int R>
 cudaError_t fused_ws_launch_r(const FusedLaunch& L, int* err) {
   using W = WsGeom<R>;
+  if (L.P.kbits != PatchConst<3, R>::K || L.P.n != PatchConst<3, R>::N)
+    return cudaErrorInvalidValue;
   auto kern = k_fused_ws<T, T, R>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)W::BYTES);
