@@ -35,7 +35,9 @@ typedef enum {
     LC2_ERR_CUDA = 3,             /* a CUDA runtime call failed */
     LC2_ERR_NOT_READY = 4,        /* images not set yet */
     LC2_ERR_SINGULAR = 5,         /* non-invertible transform */
-    LC2_ERR_UNSUPPORTED = 6       /* mode/patch size outside the supported range */
+    LC2_ERR_UNSUPPORTED = 6,      /* mode/patch size outside the supported range */
+    LC2_ERR_TIMEOUT = 7           /* a bounded device-side wait expired; the context
+                                     stays usable */
 } lc2_status;
 
 typedef enum { LC2_MODE_2D = 0, LC2_MODE_3D = 1, LC2_MODE_2DTO3D = 2 } lc2_mode;
@@ -162,8 +164,18 @@ enum { LC2_OPTION_ZCHUNK = 2, LC2_OPTION_GRAPHS = 3 };
 /* LC2_OPTION_PIPELINE: 1 runs 3D evaluations with patch radius <= 4 on the
  * warp-specialised fused kernel (producer warps resample the next slices
  * into a shared ring while consumer warps do the moments); 0 (default) the
- * single-role kernel. Same values either way. */
+ * single-role kernel. Same values either way. Every producer/consumer wait
+ * of that kernel gives up after one second: the kernel then stops its CTA,
+ * and the call that launched it (or the next lc2_fetch_results) returns
+ * LC2_ERR_TIMEOUT with the context still usable. */
 enum { LC2_OPTION_PIPELINE = 4 };
+/* Self-test of that failure path: runs the same bounded wait, for one
+ * second, on a barrier that nothing completes, on the context's stream.
+ * Returns LC2_ERR_TIMEOUT when the wait expired and was reported as it must
+ * (the expected result), LC2_OK if it did not expire; nothing faults, traps
+ * or hangs, and the context's later evaluations are unaffected. No
+ * counterpart in the reference (it checks no CUDA status at all). */
+int lc2_wait_probe(lc2_context* ctx);
 /* LC2_OPTION_STREAM_PRIORITY: recreates the context's own stream with this
  * CUDA stream priority (lower = more urgent, clamped to the device's range;
  * see cudaDeviceGetStreamPriorityRange). The server gives small requests the

@@ -23,6 +23,7 @@ STATUS_NAMES = {
     4: "LC2_ERR_NOT_READY",
     5: "LC2_ERR_SINGULAR",
     6: "LC2_ERR_UNSUPPORTED",
+    7: "LC2_ERR_TIMEOUT",
 }
 MODES = {"2D": 0, "3D": 1, "2DTo3D": 2}
 OPTION_TILE_ROWS = 1
@@ -39,7 +40,7 @@ EXPORTED = [
     "lc2_create", "lc2_destroy", "lc2_set_images", "lc2_virtual_dims", "lc2_evaluate",
     "lc2_evaluate_batch", "lc2_stage_transforms", "lc2_launch_staged", "lc2_fetch_results",
     "lc2_get_stream", "lc2_set_stream", "lc2_evaluate_fields", "lc2_launch_count",
-    "lc2_enable_kernel_timing", "lc2_kernel_times", "lc2_set_option",
+    "lc2_enable_kernel_timing", "lc2_kernel_times", "lc2_set_option", "lc2_wait_probe",
     "lc2_affine_3d", "lc2_affine_2d", "lc2_invert_affine_3d", "lc2_last_error", "lc2_version",
     "lc2_evaluate_noalloc", "lc2_minimize", "lc2_register", "lc2_params_to_matrix",
     "lc2_stack_create", "lc2_stack_destroy", "lc2_stack_set_moving", "lc2_stack_add_frame",
@@ -176,6 +177,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "lc2_evaluate_fields": ([vp, _fp, _dp, _fp, _fp, _fp, _fp, _fp], ctypes.c_int),
         "lc2_launch_count": ([vp], ctypes.c_longlong),
         "lc2_enable_kernel_timing": ([vp, ctypes.c_int], ctypes.c_int),
+        "lc2_wait_probe": ([vp], ctypes.c_int),
         "lc2_set_option": ([vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "lc2_kernel_times": ([vp, _dp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
         "lc2_affine_3d": ([_fp, _fp, _fp, _fp, _fp, _fp, _fp], ctypes.c_int),
@@ -395,6 +397,12 @@ class Context:
         _check(self._lib.lc2_autotune(self._h, m.ctypes.data_as(_fp), m.shape[0],
                                       ctypes.byref(tr), ctypes.byref(zc)))
         return tr.value, zc.value
+
+    def wait_probe(self):
+        """Self-test of the bounded device-side waits (lc2_wait_probe): raises
+        LC2Error(LC2_ERR_TIMEOUT) when the one-second wait expired and was
+        reported, as it must; the context stays usable."""
+        _check(self._lib.lc2_wait_probe(self._h))
 
     def enable_kernel_timing(self, on: bool = True):
         _check(self._lib.lc2_enable_kernel_timing(self._h, int(bool(on))))

@@ -722,7 +722,7 @@ int check_pipeline(lc2_context* c) {
   if (*c->h_err == 0) return LC2_OK;
   *c->h_err = 0;
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
-  return fail(LC2_ERR_CUDA, "pipelined kernel: a producer/consumer wait timed out");
+  return fail(LC2_ERR_TIMEOUT, "pipelined kernel: a producer/consumer wait timed out");
 }
 
 int check_ctx(const lc2_context* c) {
@@ -1039,6 +1039,18 @@ int lc2_set_option(lc2_context* c, int option, int value) {
     return LC2_OK;
   }
   return fail(LC2_ERR_INVALID_ARGUMENT, "unknown option %d", option);
+}
+
+int lc2_wait_probe(lc2_context* c) {
+  g_err.clear();
+  LC2_TRY(check_ctx(c));
+  LC2_TRY(select_device(c));
+  LC2_CUDA(cudaStreamSynchronize(c->stream));  // no earlier report pending
+  LC2_TRY(check_pipeline(c));
+  LC2_CUDA(lc2::wait_probe_launch(c->d_err, c->stream));
+  LC2_CUDA(cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  LC2_CUDA(cudaStreamSynchronize(c->stream));
+  return check_pipeline(c);
 }
 
 int lc2_enable_kernel_timing(lc2_context* c, int on) {

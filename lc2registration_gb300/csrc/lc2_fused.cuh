@@ -943,6 +943,11 @@ cudaError_t fused_launch_nd(const FusedLaunch& L) {
 template <typename T>
 cudaError_t fused_ws_launch(const FusedLaunch& L, int* err);
 
+// Self-test of the warp-specialised kernel's bounded waits: one warp waits
+// on a barrier that nothing completes until the wait's time limit raises
+// `err` (defined in lc2_fused_f32.cu).
+cudaError_t wait_probe_launch(int* err, cudaStream_t stream);
+
 template <>
 cudaError_t fused_launch<float>(const FusedLaunch& L);
 template <>

@@ -49,8 +49,9 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 // Waits for the phase of `bar` with the given parity to complete, for at most
-// one second; on expiry (or when another thread already gave up) sets the
-// abort flag and returns false.
+// one second -- or 2^26 polls, should the global timer not advance; on expiry
+// (or when another thread already gave up) sets the abort flag and returns
+// false.
 __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity,
                                           volatile int* abort_flag, int* err) {
   const unsigned addr = smem_addr(bar);
@@ -68,7 +69,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
     if (ok) return true;
     if (it == 0) {
       t0 = global_ns();
-    } else if ((it & 63) == 0 && global_ns() - t0 > 1000000000ull) {
+    } else if ((it & 63) == 0 && (global_ns() - t0 > 1000000000ull || it >= (1u << 26))) {
       *abort_flag = 1;
       atomicExch(err, 1);
       return false;
