@@ -135,8 +135,9 @@ def test_tile_heights_agree_across_sampling_bands(r):
         assert abs(ref[k] / want - 1.0) < REL_LC2, (k, ref[k], want)
 
 
-@pytest.mark.parametrize("kind", ["2d_r5", "2dto3d_r4"])
-def test_2d_tile_heights_agree_and_match_oracle(kind):
+@pytest.mark.parametrize("kind,storage", [("2d_r5", "f32"), ("2d_r6", "bf16"),
+                                          ("2dto3d_r4", "f16")])
+def test_2d_tile_heights_agree_and_match_oracle(kind, storage):
     """2D and 2D-to-3D contexts of radius 4-6 run 32-row tiles on large
     launches and 16-row tiles on small ones; both sample from the same
     32-row band, so the choice never changes a bit, and LC2 matches the
@@ -147,18 +148,20 @@ def test_2d_tile_heights_agree_and_match_oracle(kind):
 
     if kind == "2d_r5":
         case = synth.case_2d(seed=14, size=100, r=5)
+    elif kind == "2d_r6":
+        case = synth.case_2d(seed=15, size=90, r=6)
     else:
         mr = synth.mr_phantom((40, 40, 40), 6, 1.5, seed=34)
         mg = Geometry((40, 40, 40), (1, 1, 1), (0, 0, 0))
         case = synth.frame_stack(mr, mg, 1, seed=35, sides=(70,), spacing=0.5, r=4)[0]
     mats = np.concatenate([case.true_mat[None], perturbed(case, np.random.default_rng(6), 3)])
-    ctx = make_context(case)
+    ctx = make_context(case, storage)
     ref = ctx.evaluate_batch(mats)
     for rows in (32, 16, 0):
         ctx.set_option(capi.OPTION_TILE_ROWS, rows)
         np.testing.assert_array_equal(ctx.evaluate_batch(mats), ref)
         np.testing.assert_array_equal([ctx.evaluate(m) for m in mats[:2]], ref[:2])
     for k in range(len(mats)):
-        want = oracle_eval(case, mats[k], use_boxsum=False)
+        want = oracle_eval(case, mats[k], storage=storage, use_boxsum=False)
         assert want > 0.01
         assert abs(ref[k] / want - 1.0) < REL_LC2, (k, ref[k], want)
