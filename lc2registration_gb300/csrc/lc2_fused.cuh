@@ -888,7 +888,7 @@ cudaError_t fused_launch_rt(const FusedLaunch& L) {
 // Tile heights: 3D patches of radius <= 4 run 32x16 tiles (one CTA per SM),
 // 32x24 tiles (one 768-thread CTA per SM) or 32x8 tiles (two per SM); larger
 // radii only fit 32x8; 2D runs 32x32 (two 1024-thread CTAs per SM, radius
-// <= 6) or 32x16 tiles (four per SM).
+// 4-6, launches of four CTAs per SM or more) or 32x16 tiles (four per SM).
 template <int ND, int WND, typename T, int R>
 cudaError_t fused_launch_r(const FusedLaunch& L) {
   if constexpr (ND == 3 && R > 4) {
