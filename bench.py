@@ -65,6 +65,7 @@ def parse():
     ap.add_argument("--no-stack", action="store_true", help="skip the 2D-to-3D frame-stack line")
     ap.add_argument("--no-fixed", action="store_true",
                     help="skip the HighResolutionModality: Fixed lines")
+    ap.add_argument("--no-mi", action="store_true", help="skip the mutual-information lines")
     ap.add_argument("--stack-frames", type=int, default=64)
     ap.add_argument("--stack-poses", type=int, default=256)
     ap.add_argument("--serve-requests", type=int, default=48)
@@ -451,6 +452,56 @@ def stack_leg(args, main_case, device):
                     "f16 storage, 7x7 patches, one graph-replayed launch per call"}
 
 
+def mi_leg(args, main_case, device):
+    """Normalised mutual information (PatchSize 0; cu_lc2_3d.cu:868-923,
+    1196-1301): device-timed batches and one lc2_evaluate per transform, on
+    the main 256^3 volumes (f16) and on the 128^3 -> 96^3 case (f32). NMI >= 1
+    always; batched and plain values must agree bit for bit."""
+    import numpy as np
+    import torch
+
+    from lc2registration_gb300 import capi, synth
+    from tests.helpers import perturbed
+
+    out = {}
+    for name, case, storage, K in (
+            ("3d_256_f16", main_case, "f16", 64),
+            ("3d_128_96", synth.case_3d(seed=8, mr_size=128, us_size=96, r=3), "f32", 256)):
+        ctx = capi.Context(case.mode, case.fixed_geom, case.moving_geom, case.virt_spacing, 0,
+                           True, storage, device=device)
+        ctx.set_images(case.fixed, case.moving)
+        mats = perturbed(case, np.random.default_rng(5), K)
+        ctx.stage(mats)
+        stream = torch.cuda.ExternalStream(ctx.stream())
+        for _ in range(2):
+            ctx.launch(K)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        reps = 3
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for _ in range(reps):
+            ctx.launch(K)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        batched = reps * K / (ev[0].elapsed_time(ev[1]) / 1e3)
+        vals = ctx.fetch(K)
+        assert np.all(np.isfinite(vals)) and vals.min() >= 1.0, "NMI out of range"
+        for m in mats[:4]:
+            ctx.evaluate(m)
+        n = 32
+        t0 = time.perf_counter()
+        plain = [ctx.evaluate(m) for m in mats[:n]]
+        plain_eps = n / (time.perf_counter() - t0)
+        assert np.array_equal(np.array(plain), vals[:n]), "plain != batched"
+        nv = int(np.prod(ctx.virtual_dims()))
+        out[name] = {"batched_evals_per_s": batched, "plain_evals_per_s": plain_eps,
+                     "batched_over_plain": batched / plain_eps, "candidates_per_launch": K,
+                     "virtual_voxels": nv, "voxel_evals_per_s": batched * nv,
+                     "storage": storage}
+        ctx.close()
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -636,6 +687,9 @@ def main():
     stack = None
     if rank == 0 and not args.no_stack:
         stack = stack_leg(args, case, local)
+    mi = None
+    if rank == 0 and not args.no_mi:
+        mi = mi_leg(args, case, local)
     serve = None
     if rank == 0 and not args.no_serve:
         serve = serve_leg(args, case, local)
@@ -662,6 +716,7 @@ def main():
             "small_configs": small,
             "fixed_modality": fixed,
             "stack": stack,
+            "mutual_information": mi,
             "serve": serve,
             "gpu_launches": launches,
             "clocks": clk.summary(),

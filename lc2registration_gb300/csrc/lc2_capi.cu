@@ -171,6 +171,7 @@ struct lc2_context {
   bool mi = false;
   unsigned char* d_sbin = nullptr;
   unsigned* d_hist = nullptr;
+  double* d_mipart = nullptr;  // entropy sums per part of each histogram
   unsigned* d_rmin = nullptr;
   unsigned* d_rmax = nullptr;
   double h_static = 0.0;
@@ -393,10 +394,13 @@ int ensure_capacity(lc2_context* c, int count) {
   LC2_CUDA(host_alloc((void**)&c->h_out, sizeof(double) * ncap));
   if (c->mi) {
     dev_free(c->d_hist, c->stream);
+    dev_free(c->d_mipart, c->stream);
     dev_free(c->d_rmin, c->stream);
     dev_free(c->d_rmax, c->stream);
-    c->d_hist = nullptr; c->d_rmin = nullptr; c->d_rmax = nullptr;
+    c->d_hist = nullptr; c->d_mipart = nullptr; c->d_rmin = nullptr; c->d_rmax = nullptr;
     LC2_CUDA(dev_alloc((void**)&c->d_hist, sizeof(unsigned) * lc2::kMiHist * (size_t)ncap, c->stream));
+    LC2_CUDA(dev_alloc((void**)&c->d_mipart, sizeof(double) * 2 * lc2::kMiParts * (size_t)ncap,
+                       c->stream));
     LC2_CUDA(dev_alloc((void**)&c->d_rmin, sizeof(unsigned) * ncap, c->stream));
     LC2_CUDA(dev_alloc((void**)&c->d_rmax, sizeof(unsigned) * ncap, c->stream));
   }
@@ -672,11 +676,16 @@ int launch_mi(lc2_context* c, int cnt) {
   LC2_CUDA(cudaMemsetAsync(c->d_rmax, 0x00, sizeof(unsigned) * cnt, c->stream));
   LC2_CUDA(cudaMemsetAsync(c->d_hist, 0, sizeof(unsigned) * lc2::kMiHist * (size_t)cnt, c->stream));
   dim3 block(32, 8, 1);
-  // one launch covers at most 65535 / vz transforms (grid z limit)
-  const int per = std::max(1, 65535 / v.dim[2]);
-  for (int k0 = 0; k0 < cnt; k0 += per) {
-    const int n = std::min(per, cnt - k0);
-    dim3 grid((v.dim[0] + 31) / 32, (v.dim[1] + 7) / 8, v.dim[2] * n);
+  const long long tiles = (long long)((v.dim[0] + 31) / 32) * ((v.dim[1] + 7) / 8);
+  // slices per CTA: up to kMiChunk, fewer where the launch would otherwise
+  // have under eight CTAs per SM (one small transform)
+  const long long work = tiles * v.dim[2] * (long long)std::min(cnt, 65535);
+  P.zchunk = (int)std::max(1LL, std::min<long long>(lc2::kMiChunk, work / (8LL * c->sms)));
+  const int chunks = (v.dim[2] + P.zchunk - 1) / P.zchunk;
+  // one launch covers at most 65535 transforms (grid z / y limit)
+  for (int k0 = 0; k0 < cnt; k0 += 65535) {
+    const int n = std::min(65535, cnt - k0);
+    dim3 grid((unsigned)tiles, chunks, n);
     TimerScope ts(c, K_MOMENTS);
     const int st = c->cfg.storage;
     if (st == LC2_STORE_F16) {
@@ -689,11 +698,13 @@ int launch_mi(lc2_context* c, int cnt) {
       lc2::k_mi_range<float><<<grid, block, 0, c->stream>>>((const float*)c->d_moving, P, c->d_xf, k0, c->d_rmin, c->d_rmax);
       lc2::k_mi_hist<float><<<grid, block, 0, c->stream>>>((const float*)c->d_moving, P, c->d_xf, k0, c->d_sbin, c->d_rmin, c->d_rmax, c->d_hist);
     }
-    c->launches += 2;
+    lc2::k_mi_part<<<dim3(lc2::kMiParts, n), 256, 0, c->stream>>>(c->d_hist, k0,
+                                                                  P.warped_is_high_res, c->d_mipart);
+    c->launches += 3;
     LC2_CUDA(cudaGetLastError());
   }
-  lc2::k_mi_nmi<<<cnt, 1024, 0, c->stream>>>(c->d_hist, 0, P.warped_is_high_res, c->h_static,
-                                              (double)c->nv, c->d_out);
+  lc2::k_mi_nmi<<<(cnt + 127) / 128, 128, 0, c->stream>>>(c->d_mipart, cnt, c->h_static,
+                                                          (double)c->nv, c->d_out);
   ++c->launches;
   LC2_CUDA(cudaGetLastError());
   return LC2_OK;
@@ -837,7 +848,8 @@ void context_bytes(const lc2_context* c, size_t* held, size_t* peak_extra) {
   if (!hrm) h += c->nv * sizeof(float);        // its Sobel
   if (hrm && !c->mi) h += c->nv * (sizeof(float) + sizeof(int));  // weighting factors, S_U
   if (!hrm && !c->mi) h += c->nv * (4 * sizeof(int) + 3 * sizeof(long long));  // static sums
-  if (c->mi) h += c->nv + 64 * (sizeof(unsigned) * (lc2::kMiHist + 2));
+  if (c->mi)
+    h += c->nv + 64 * (sizeof(unsigned) * (lc2::kMiHist + 2) + sizeof(double) * 2 * lc2::kMiParts);
   h += 64 * (sizeof(lc2::Xform) + 2 * sizeof(unsigned long long) + sizeof(double));
   *held = h;
   *peak_extra = std::max(c->nm, c->nf) * sizeof(float);
@@ -944,6 +956,7 @@ int lc2_destroy(lc2_context* c) {
   dev_free(c->d_scratch, fs);
   dev_free(c->d_sbin, fs);
   dev_free(c->d_hist, fs);
+  dev_free(c->d_mipart, fs);
   dev_free(c->d_rmin, fs);
   dev_free(c->d_rmax, fs);
   dev_free(c->d_xf, fs);
