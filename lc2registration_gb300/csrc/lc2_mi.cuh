@@ -33,6 +33,7 @@ struct MiParams {
   int vx, vy, vz;         // virtual grid
   int warped_is_high_res; // 1: key = static bin + 256 * warped bin; 0: the transpose
   int zchunk;             // slices per range / histogram CTA, <= kMiChunk
+  int table;              // k_mi_hist merges counts in a shared table first
 };
 
 // Order-preserving float <-> unsigned maps for atomicMin / atomicMax.
@@ -112,8 +113,34 @@ __global__ void __launch_bounds__(256) k_mi_range(const TM* __restrict__ mov, Mi
   }
 }
 
+// Shared aggregation table of k_mi_hist: (key, count) slots filled by
+// open addressing; a key that finds no slot within kMiProbes probes goes
+// straight to the global histogram, so every count lands exactly once.
+constexpr int kMiTable = 2048;
+constexpr int kMiProbes = 32;
+
+__device__ __forceinline__ void mi_table_add(int* tkey, unsigned* tcnt, unsigned* h, int key,
+                                             unsigned n) {
+  int slot = (int)(((unsigned)key * 2654435761u) >> 21);  // 11-bit Fibonacci hash
+  for (int i = 0; i < kMiProbes; ++i) {
+    int k = *(volatile int*)&tkey[slot];
+    if (k == -1) {
+      k = atomicCAS(&tkey[slot], -1, key);
+      if (k == -1) k = key;  // this thread claimed the slot
+    }
+    if (k == key) {
+      atomicAdd(&tcnt[slot], n);
+      return;
+    }
+    slot = (slot + 1) & (kMiTable - 1);
+  }
+  atomicAdd(h + key, n);
+}
+
 // Joint histogram of each transform: static bins sbin (uint8 per voxel) and
-// the warped image's bins in its range. Grid and block as k_mi_range.
+// the warped image's bins in its range. Grid and block as k_mi_range. With
+// P.table a CTA first merges its counts in a shared table (neighbouring
+// voxels share bins), then adds each key once.
 template <typename TM>
 __global__ void __launch_bounds__(256) k_mi_hist(const TM* __restrict__ mov, MiParams P,
                                                  const Xform* __restrict__ xf, int k0,
@@ -122,10 +149,20 @@ __global__ void __launch_bounds__(256) k_mi_hist(const TM* __restrict__ mov, MiP
                                                  const unsigned* __restrict__ rmax,
                                                  unsigned* __restrict__ hist) {
   __shared__ TileBase T[kMiChunk];
+  __shared__ int tkey[kMiTable];
+  __shared__ unsigned tcnt[kMiTable];
   const int ntx = (P.vx + 31) / 32;
   const int x0 = (blockIdx.x % ntx) * 32, y0 = (blockIdx.x / ntx) * 8;
   const int zb = blockIdx.y * P.zchunk, ze = min(zb + P.zchunk, P.vz);
   const int slot = blockIdx.z;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  const bool table = P.table != 0;
+  if (table) {
+    for (int i = tid; i < kMiTable; i += 256) {
+      tkey[i] = -1;
+      tcnt[i] = 0;
+    }
+  }
   mi_bases(xf + k0 + slot, x0, y0, zb, ze, T);
   __syncthreads();
   const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
@@ -145,7 +182,17 @@ __global__ void __launch_bounds__(256) k_mi_hist(const TM* __restrict__ mov, MiP
     }
     // voxels of a warp that share a bin add once
     const unsigned peers = __match_any_sync(0xffffffffu, key);
-    if (key >= 0 && lane == __ffs(peers) - 1) atomicAdd(h + key, (unsigned)__popc(peers));
+    if (key >= 0 && lane == __ffs(peers) - 1) {
+      if (table)
+        mi_table_add(tkey, tcnt, h, key, (unsigned)__popc(peers));
+      else
+        atomicAdd(h + key, (unsigned)__popc(peers));
+    }
+  }
+  if (table) {
+    __syncthreads();
+    for (int i = tid; i < kMiTable; i += 256)
+      if (tkey[i] >= 0) atomicAdd(h + tkey[i], tcnt[i]);
   }
 }
 
