@@ -366,7 +366,7 @@ __device__ __forceinline__ float fused_measure(const FusedParams& P, float sg, i
 }
 
 // Square root of a Sobel magnitude: PTX sqrt.approx (one instruction, a
-// couple of ulp). The magnitude is quantised at 2^-19 of its range next, so
+// couple of ulp). The magnitude is quantised at 2^-20 of its range or finer next, so
 // the approximation never moves a quantised value by more than one step and
 // LC2 by far less than 1e-7.
 __device__ __forceinline__ float sqrt_approx(float x) {
