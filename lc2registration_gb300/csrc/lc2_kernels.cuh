@@ -222,6 +222,47 @@ __device__ __forceinline__ float tile_sample(const TM* __restrict__ mov, int mx,
   return fmaf(ax.r, xr - xl, xl);
 }
 
+// Whether every sample of a 32 x 8 tile slice from base T lies strictly
+// inside the moving volume (0 <= floor, floor + 1 <= dim - 1 on each axis):
+// the tile's corners bound the affine image, 0.01 voxel covers float rounding.
+__device__ __forceinline__ bool tile_inside(const TileBase& T, int mx, int my, int mz) {
+  const int dims[3] = {mx, my, mz};
+  bool in = true;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float ex = T.A[3 * a] * 31.0f, ey = T.A[3 * a + 1] * 7.0f;
+    const float lo = T.fb[a] + fminf(ex, 0.0f) + fminf(ey, 0.0f);
+    const float hi = T.fb[a] + fmaxf(ex, 0.0f) + fmaxf(ey, 0.0f);
+    in = in && ((float)T.ib[a] + lo >= 0.01f) && ((float)T.ib[a] + hi <= (float)(dims[a] - 1) - 0.01f);
+  }
+  return in;
+}
+
+// tile_sample<3> for a tile slice that tile_inside accepted: no bounds tests,
+// the ceil corner always floor + 1 -- where the fraction is 0 its weight is
+// 0 -- so the value equals tile_sample's bit for bit.
+template <typename TM>
+__device__ __forceinline__ float tile_sample_inside(const TM* __restrict__ mov, int mx, int my,
+                                                    const TileBase& T, int tx, int ty) {
+  const float dx = (float)tx, dy = (float)ty;
+  const float qx = fmaf(T.A[1], dy, fmaf(T.A[0], dx, T.fb[0]));
+  const float qy = fmaf(T.A[4], dy, fmaf(T.A[3], dx, T.fb[1]));
+  const float qz = fmaf(T.A[7], dy, fmaf(T.A[6], dx, T.fb[2]));
+  const float flx = floorf(qx), fly = floorf(qy), flz = floorf(qz);
+  const float rx = qx - flx, ry = qy - fly, rz = qz - flz;
+  const unsigned umx = (unsigned)mx, mxy = (unsigned)mx * (unsigned)my;
+  const unsigned b = (unsigned)(T.ib[0] + (int)flx) + (unsigned)(T.ib[1] + (int)fly) * umx +
+                     (unsigned)(T.ib[2] + (int)flz) * mxy;
+  float lu0 = ldf(mov, b), lu1 = ldf(mov, b + mxy);
+  float ru0 = ldf(mov, b + 1), ru1 = ldf(mov, b + 1 + mxy);
+  float rb0 = ldf(mov, b + 1 + umx), rb1 = ldf(mov, b + 1 + umx + mxy);
+  float lb0 = ldf(mov, b + umx), lb1 = ldf(mov, b + umx + mxy);
+  float lu = fmaf(rz, lu1 - lu0, lu0), ru = fmaf(rz, ru1 - ru0, ru0);
+  float rb = fmaf(rz, rb1 - rb0, rb0), lb = fmaf(rz, lb1 - lb0, lb0);
+  float l = fmaf(ry, lb - lu, lu), r = fmaf(ry, rb - ru, ru);
+  return fmaf(rx, r - l, l);
+}
+
 // One CTA = 32x8 virtual voxels of one z-slice of one transform slot.
 template <int ND, typename TM>
 __global__ void __launch_bounds__(256) k_warp(const TM* __restrict__ mov, int mx, int my, int mz,

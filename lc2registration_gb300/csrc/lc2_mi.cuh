@@ -60,11 +60,22 @@ constexpr int kMiChunk = 64;  // most slices per range / histogram CTA
 constexpr int kMiParts = 32;  // entropy CTAs per transform (8 warped bins each)
 
 // Sampling bases of a CTA's tile for its slices [zb, ze), one per thread, in
-// shared memory; the caller synchronises.
-__device__ __forceinline__ void mi_bases(const Xform* X, int x0, int y0, int zb, int ze,
-                                         TileBase* T) {
+// shared memory, and whether each slice samples strictly inside the warped
+// image (tile_inside); the caller synchronises.
+__device__ __forceinline__ void mi_bases(const Xform* X, const MiParams& P, int x0, int y0,
+                                         int zb, int ze, TileBase* T, int* inside) {
   const int t = threadIdx.y * blockDim.x + threadIdx.x;
-  if (zb + t < ze) tile_base(X, x0, y0, zb + t, T[t]);
+  if (zb + t < ze) {
+    tile_base(X, x0, y0, zb + t, T[t]);
+    inside[t] = tile_inside(T[t], P.mx, P.my, P.mz) ? 1 : 0;
+  }
+}
+
+template <typename TM>
+__device__ __forceinline__ float mi_sample(const TM* __restrict__ mov, const MiParams& P,
+                                           const TileBase& T, int inside) {
+  return inside ? tile_sample_inside<TM>(mov, P.mx, P.my, T, threadIdx.x, threadIdx.y)
+                : tile_sample<3, TM>(mov, P.mx, P.my, P.mz, T, threadIdx.x, threadIdx.y);
 }
 
 // Range of the warped image of each transform. Grid (tiles of 32 x 8, z
@@ -75,18 +86,19 @@ __global__ void __launch_bounds__(256) k_mi_range(const TM* __restrict__ mov, Mi
                                                   unsigned* __restrict__ rmin,
                                                   unsigned* __restrict__ rmax) {
   __shared__ TileBase T[kMiChunk];
+  __shared__ int inside[kMiChunk];
   __shared__ float red[2][8];
   const int ntx = (P.vx + 31) / 32;
   const int x0 = (blockIdx.x % ntx) * 32, y0 = (blockIdx.x / ntx) * 8;
   const int zb = blockIdx.y * P.zchunk, ze = min(zb + P.zchunk, P.vz);
   const int slot = blockIdx.z;
-  mi_bases(xf + k0 + slot, x0, y0, zb, ze, T);
+  mi_bases(xf + k0 + slot, P, x0, y0, zb, ze, T, inside);
   __syncthreads();
   const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
   float lo = INFINITY, hi = -INFINITY;
   if (x < P.vx && y < P.vy) {
     for (int z = zb; z < ze; ++z) {
-      const float v = tile_sample<3, TM>(mov, P.mx, P.my, P.mz, T[z - zb], threadIdx.x, threadIdx.y);
+      const float v = mi_sample<TM>(mov, P, T[z - zb], inside[z - zb]);
       lo = fminf(lo, v);
       hi = fmaxf(hi, v);
     }
@@ -149,6 +161,7 @@ __global__ void __launch_bounds__(256) k_mi_hist(const TM* __restrict__ mov, MiP
                                                  const unsigned* __restrict__ rmax,
                                                  unsigned* __restrict__ hist) {
   __shared__ TileBase T[kMiChunk];
+  __shared__ int inside[kMiChunk];
   __shared__ int tkey[kMiTable];
   __shared__ unsigned tcnt[kMiTable];
   const int ntx = (P.vx + 31) / 32;
@@ -163,7 +176,7 @@ __global__ void __launch_bounds__(256) k_mi_hist(const TM* __restrict__ mov, MiP
       tcnt[i] = 0;
     }
   }
-  mi_bases(xf + k0 + slot, x0, y0, zb, ze, T);
+  mi_bases(xf + k0 + slot, P, x0, y0, zb, ze, T, inside);
   __syncthreads();
   const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
   const bool in = x < P.vx && y < P.vy;
@@ -174,7 +187,7 @@ __global__ void __launch_bounds__(256) k_mi_hist(const TM* __restrict__ mov, MiP
   for (int z = zb; z < ze; ++z) {
     int key = -1;
     if (in) {
-      const float v = tile_sample<3, TM>(mov, P.mx, P.my, P.mz, T[z - zb], threadIdx.x, threadIdx.y);
+      const float v = mi_sample<TM>(mov, P, T[z - zb], inside[z - zb]);
       const int wb = mi_bin(v, lo, sc);
       const int sb = sbin[((size_t)z * P.vy + y) * P.vx + x];
       if (wb >= 0 && wb < kMiBins)
