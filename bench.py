@@ -36,6 +36,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -66,6 +68,7 @@ def parse():
     ap.add_argument("--no-fixed", action="store_true",
                     help="skip the HighResolutionModality: Fixed lines")
     ap.add_argument("--no-mi", action="store_true", help="skip the mutual-information lines")
+    ap.add_argument("--no-bf16", action="store_true", help="skip the bf16-storage line")
     ap.add_argument("--stack-frames", type=int, default=64)
     ap.add_argument("--stack-poses", type=int, default=256)
     ap.add_argument("--serve-requests", type=int, default=48)
@@ -159,18 +162,33 @@ class ClockSampler:
 
 
 def cpu_port(case, mats, seconds: float, storage: str):
-    """FP64 oracle on the host cores over a bounded sample of candidates."""
+    """FP64 oracle on the host cores over a bounded sample of candidates.
+    Returns the rate, the count, the seconds and the oracle's LC2 values (in
+    transform order), which the caller checks the GPU results against."""
     from tests.helpers import oracle_eval
 
     t0 = time.perf_counter()
-    done = 0
+    vals = []
     while True:
-        oracle_eval(case, mats[done % len(mats)], storage=storage)
-        done += 1
+        vals.append(oracle_eval(case, mats[len(vals) % len(mats)], storage=storage))
         el = time.perf_counter() - t0
-        if el >= seconds and done >= 2:
+        if el >= seconds and len(vals) >= 2:
             break
-    return done / el, done, el
+    return len(vals) / el, len(vals), el, np.array(vals[: len(mats)])
+
+
+def parity_vs_oracle(gpu_vals, oracle_vals, tol=1e-5):
+    """Largest relative LC2 difference between the GPU's values and the FP64
+    oracle's on the same transforms (the oracle fed the same storage-rounded
+    volumes); raises when it exceeds tol, so a bench line is never printed
+    for results that differ from the oracle."""
+    g = np.asarray(gpu_vals[: len(oracle_vals)], dtype=np.float64)
+    o = np.asarray(oracle_vals, dtype=np.float64)
+    rel = np.abs(g - o) / np.maximum(np.abs(o), 1e-300)
+    worst = float(rel.max()) if len(rel) else None
+    if worst is not None and not worst < tol:
+        raise AssertionError(f"GPU vs FP64 oracle: max relative LC2 error {worst:.3e} > {tol}")
+    return {"max_rel_err_vs_oracle": worst, "evaluations_checked": int(len(o)), "tolerance": tol}
 
 
 def _registration(case, rng):
@@ -319,15 +337,60 @@ def small_configs(device):
         plain = [ctx.evaluate(m) for m in mats[:n % K or K][:n]]
         plain_eps = len(plain) / (time.perf_counter() - t0)
         assert np.array_equal(np.array(plain), vals[:len(plain)]), "plain != batched"
+        nv = int(np.prod(ctx.virtual_dims()))
+        # algorithmic bytes (f32): K N s_mov + N s_fix per batched launch, N (s_mov
+        # + s_fix) per plain evaluation
         out[name] = {"batched_evals_per_s": batched, "plain_evals_per_s": plain_eps,
                      "plain_latency_ms": 1e3 / plain_eps,
                      "batched_over_plain": batched / plain_eps, "candidates_per_launch": K,
-                     "virtual_voxels": int(np.prod(ctx.virtual_dims())), "storage": "f32"}
+                     "virtual_voxels": nv, "storage": "f32",
+                     "algorithmic_gbs_batched": (K * nv * 4 + nv * 4) * batched / K / 1e9,
+                     "algorithmic_gbs_plain": nv * 8 * plain_eps / 1e9}
         ctx.close()
     return out
 
 
-def issue_roofline(ipv, voxels, kernel_ms, device, clk):
+def bf16_leg(args, case, mats, device, flush):
+    """The main workload with both volumes held in bf16 instead of f16: the
+    same 512-transform launches, device-timed with L2 flushed between them,
+    and two of the transforms checked against the FP64 oracle fed the same
+    bf16-rounded volumes."""
+    import torch
+
+    from lc2registration_gb300 import capi
+    from tests.helpers import oracle_eval
+
+    ctx = capi.Context(case.mode, case.fixed_geom, case.moving_geom, case.virt_spacing, case.r,
+                       case.hr_moving, "bf16", device=device)
+    ctx.set_images(case.fixed, case.moving)
+    K = mats.shape[0]
+    ctx.stage(mats)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    for _ in range(2):
+        ctx.launch(K)
+    reps = 3
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(reps)]
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for i in range(reps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            ctx.launch(K)
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / reps
+    vals = ctx.fetch(K)
+    ctx.close()
+    out = {"batched_evals_per_s": K / (ms / 1e3), "ms_per_launch": ms,
+           "candidates_per_launch": K, "storage": "bf16"}
+    if not args.no_cpu:
+        ovals = [oracle_eval(case, mats[i], storage="bf16") for i in (0, K - 1)]
+        out["parity"] = parity_vs_oracle(vals[[0, K - 1]], ovals)
+    return out
+
+
+def issue_roofline(ipv, voxels, kernel_ms, device, clk, source):
     """The bound the fused kernel actually meets: instruction issue. achieved =
     warp instructions of one launch (ncu's per-voxel count x voxels / 32) per
     second of the event-timed launch; peak = SMs x 4 schedulers x one warp
@@ -342,7 +405,7 @@ def issue_roofline(ipv, voxels, kernel_ms, device, clk):
     peak = sms * 4 * mhz * 1e6
     return {"bound": "issue", "unit": "warp instructions/s", "achieved": achieved, "peak": peak,
             "frac": achieved / peak,
-            "source": "instructions per voxel from profiles/k_fused_traffic.json (ncu)"}
+            "source": "instructions per voxel " + source + "; launch time measured in this run"}
 
 
 def fixed_leg(args, main_case, device):
@@ -417,7 +480,8 @@ def stack_leg(args, main_case, device):
     """2D-to-3D frame stack: frames of uneven sizes (sides 128-512 at 0.5 mm)
     cut from the 256^3 MR at seeded 6-DOF poses, `stack_poses` candidate
     poses per frame, all (frame, pose) pairs in one lc2_stack_evaluate call
-    (one persistent launch, replayed from a CUDA graph after the first)."""
+    (one persistent launch, replayed from a CUDA graph after the first). The
+    MR is held in f32 (the configuration's storage) and, second line, f16."""
     import numpy as np
 
     from lc2registration_gb300 import capi, synth
@@ -425,31 +489,39 @@ def stack_leg(args, main_case, device):
 
     frames = synth.frame_stack(main_case.moving, main_case.moving_geom, args.stack_frames,
                                seed=91, spacing=0.5, r=3)
-    st = capi.Stack(main_case.moving_geom, 3, "f16", device)
-    st.set_moving(main_case.moving)
     rng = np.random.default_rng(92)
     ids, mats = [], []
     for i, f in enumerate(frames):
-        st.add_frame(f.fixed_geom, f.virt_spacing, f.fixed)
         ids += [i] * args.stack_poses
         mats.append(perturbed(f, rng, args.stack_poses, scale=0.5))
     ids = np.array(ids, dtype=np.int32)
     mats = np.concatenate(mats)
-    st.evaluate(ids, mats)  # capture
-    reps = 3
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        vals = st.evaluate(ids, mats)
-    el = (time.perf_counter() - t0) / reps
-    assert np.all(np.isfinite(vals)) and vals.max() > 0
     px = sum(int(f.fixed_geom.dim[0]) * int(f.fixed_geom.dim[1]) for f in frames)
-    st.close()
-    return {"frames": len(frames), "poses_per_frame": args.stack_poses,
-            "evaluations_per_call": int(len(ids)), "frame_pixels": px,
-            "evals_per_s": len(ids) / el, "ms_per_call": el * 1e3,
-            "pixel_evals_per_s": px * args.stack_poses / el,
-            "note": "end to end through lc2_stack_evaluate (host poses in, host LC2 out), "
-                    "f16 storage, 7x7 patches, one graph-replayed launch per call"}
+    out = {"frames": len(frames), "poses_per_frame": args.stack_poses,
+           "evaluations_per_call": int(len(ids)), "frame_pixels": px,
+           "note": "end to end through lc2_stack_evaluate (host poses in, host LC2 out), "
+                   "7x7 patches, one graph-replayed launch per call"}
+    for storage in ("f32", "f16"):
+        st = capi.Stack(main_case.moving_geom, 3, storage, device)
+        st.set_moving(main_case.moving)
+        for f in frames:
+            st.add_frame(f.fixed_geom, f.virt_spacing, f.fixed)
+        st.evaluate(ids, mats)  # capture
+        reps = 3
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            vals = st.evaluate(ids, mats)
+        el = (time.perf_counter() - t0) / reps
+        assert np.all(np.isfinite(vals)) and vals.max() > 0
+        st.close()
+        s_mov = 4 if storage == "f32" else 2
+        # algorithmic bytes: every frame pixel reads one moving element per pose
+        # and one ultrasound element (f32) per call
+        alg = px * args.stack_poses * s_mov + px * 4
+        out[f"mr_{storage}"] = {"evals_per_s": len(ids) / el, "ms_per_call": el * 1e3,
+                                "pixel_evals_per_s": px * args.stack_poses / el,
+                                "algorithmic_gbs": alg / el / 1e9}
+    return out
 
 
 def mi_leg(args, main_case, device):
@@ -621,7 +693,7 @@ def main():
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     # the reference's own kernels on this GPU type, measured separately by
-    # oracle/ref_golden/ref_gpu_time.py (profiles/reference_gpu_kernels.md)
+    # oracle/ref_golden/ref_gpu_time.py
     ref_gpu = None
     rfile = os.path.join(ROOT, "profiles", "reference_gpu_kernels.json")
     if os.path.exists(rfile):
@@ -632,20 +704,26 @@ def main():
                 ref_gpu = {"ms_per_eval": row["ms_per_eval"],
                            "evals_per_s": 1e3 / row["ms_per_eval"], "storage": "f32",
                            "lc2": row["lc2"],
-                           "source": "profiles/reference_gpu_kernels.json (one plain evaluation "
-                                     "of the reference's kernels, CUDA events, same GPU type)"}
+                           "source": "from profiles/reference_gpu_kernels.json, not measured in "
+                                     "this run (one plain evaluation of the reference's kernels "
+                                     "by oracle/ref_golden/ref_gpu_time.py, CUDA events, same "
+                                     "GPU type)"}
         except Exception:
             ref_gpu = None
     traffic = None
     ipv = None  # thread instructions per output voxel of the fused kernel (ncu)
+    captured = None
     tfile = os.path.join(ROOT, "profiles", "k_fused_traffic.json")
     if os.path.exists(tfile):
         try:
             tj = json.load(open(tfile))
             traffic = tj.get("bytes_per_launch_scaled")
             ipv = tj.get("thread_instructions_per_voxel")
+            captured = tj.get("captured_at")
         except Exception:
             traffic = None
+    from_profile = ("from profiles/k_fused_traffic.json (ncu capture of the kernel"
+                    + (f", {captured})" if captured else ")"))
 
     # ---- e2e through the public call, host buffers ----
     e2e_t = 0.0
@@ -669,18 +747,25 @@ def main():
     assert np.array_equal(np.array(plain_vals), res[:P]), "plain != batched"
 
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O
 
         O.build()
-        eps, n, el = cpu_port(case, mats, args.cpu_seconds, args.storage)
+        eps, n, el, ovals = cpu_port(case, mats, args.cpu_seconds, args.storage)
         cpu = {"value": eps, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                "sample": f"{n} full {args.size}^3 evaluations of the FP64 oracle over "
                          f"{el:.1f} s (OpenMP, all host cores); the reference has no CPU LC2 path"}
+        parity = parity_vs_oracle(res, ovals)
+        parity["note"] = (f"the first {len(ovals)} of the step's {K} transforms, GPU batch values "
+                          f"vs the FP64 oracle on the same {args.storage}-rounded volumes")
 
     small = None
     if rank == 0 and not args.no_small:
         small = small_configs(local)
+    bf16 = None
+    if rank == 0 and not args.no_bf16 and args.storage == "f16":
+        bf16 = bf16_leg(args, case, mats, local, flush)
     fixed = None
     if rank == 0 and not args.no_fixed:
         fixed = fixed_leg(args, case, local)
@@ -703,17 +788,20 @@ def main():
                                                                   "zchunk": tuned[1]}),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
+                         "traffic_source": from_profile,
                          "kernel": "k_fused", "kernel_ms_per_launch": mom_ms / max(1, mom_launches),
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
-            "issue_roofline": issue_roofline(ipv, K * n_vox, mom_ms, local, clk),
+            "issue_roofline": issue_roofline(ipv, K * n_vox, mom_ms, local, clk, from_profile),
             "kernels_ms_per_step": {k: v[0] for k, v in kt.items()},
             "cpu_baseline": cpu,
+            "parity": parity,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": K * 96,
                     "d2h_bytes_per_step": K * 8},
             "plain": {"value": plain_eps, "unit": UNIT, "evals": P,
                       "batched_over_plain": value / world / plain_eps},
             "reference_gpu_kernels": ref_gpu,
             "small_configs": small,
+            "bf16_storage": bf16,
             "fixed_modality": fixed,
             "stack": stack,
             "mutual_information": mi,

@@ -463,11 +463,15 @@ long long lc2_stack_graph_launches(const lc2_stack* s);
  * sums live in one static device array of 256 B + 8 B per voxel for at most
  * LC2_NOALLOC_MAX_VOXELS virtual voxels (8 MiB), which every GPU that loads
  * the library holds until the process exits; larger grids are rejected with
- * LC2_ERR_UNSUPPORTED. The first call on a device looks up that array's
- * device address (cudaGetSymbolAddress, with the device current), so make
- * it before any stream capture. Every call shares the array: calls that
- * overlap on the GPU (other streams, other host threads on the same device)
- * race and must be serialised by the caller. */
+ * LC2_ERR_UNSUPPORTED, as are moving images of more than 2^31 - 1 voxels.
+ * The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress, with the device current, in the device's primary
+ * context; a cudaDeviceReset invalidates it for the rest of the process).
+ * Every call blocks the host on a read-back of the input maxima, so none can
+ * be recorded into a CUDA graph: on a capturing stream the call returns
+ * LC2_ERR_UNSUPPORTED before enqueuing anything. Every call shares the
+ * array: calls that overlap on the GPU (other streams, other host threads on
+ * the same device) race and must be serialised by the caller. */
 #define LC2_NOALLOC_MAX_VOXELS (1 << 20)
 int lc2_evaluate_noalloc(int mode, const lc2_geometry* virt, const lc2_geometry* moving,
                          int patch_size, const float* d_ultrasound, const float* d_moving,

@@ -79,7 +79,9 @@ __global__ void k_ratio(const unsigned long long* __restrict__ acc, double* __re
 }
 
 // Device address of the scratch array, looked up once per device with that
-// device current.
+// device current. The address belongs to the device's primary context (the
+// one the runtime API uses); a cudaDeviceReset invalidates it, after which
+// this library must not be called again in the process.
 int scratch_for_current_device(unsigned char** out) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
@@ -132,11 +134,30 @@ extern "C" int lc2_evaluate_noalloc(int mode, const lc2_geometry* virt, const lc
   if ((mode == LC2_MODE_2D && (virt->dim[2] != 1 || moving->dim[2] != 1)) ||
       (mode == LC2_MODE_2DTO3D && virt->dim[2] != 1))
     return fail(LC2_ERR_INVALID_ARGUMENT, "2D grids need dim[2] = 1");
-  const size_t nv = (size_t)virt->dim[0] * virt->dim[1] * virt->dim[2];
-  const size_t nm = (size_t)moving->dim[0] * moving->dim[1] * moving->dim[2];
-  if (nv > (size_t)LC2_NOALLOC_MAX_VOXELS)
-    return fail(LC2_ERR_UNSUPPORTED,
-                "virtual grid larger than LC2_NOALLOC_MAX_VOXELS voxels: use lc2_create");
+  // voxel counts built one axis at a time against their limits, so no
+  // product can wrap: the virtual grid must fit the scratch array, the moving
+  // image the kernels' 32-bit gather indices
+  size_t nv = 1, nm = 1;
+  for (int a = 0; a < 3; ++a) {
+    nv *= (size_t)virt->dim[a];  // <= 2^20 * (2^31 - 1): no wrap
+    if (nv > (size_t)LC2_NOALLOC_MAX_VOXELS)
+      return fail(LC2_ERR_UNSUPPORTED,
+                  "virtual grid larger than LC2_NOALLOC_MAX_VOXELS voxels: use lc2_create");
+    nm *= (size_t)moving->dim[a];  // <= (2^31 - 1)^2: no wrap
+    if (nm > (size_t)INT32_MAX)
+      return fail(LC2_ERR_UNSUPPORTED,
+                  "moving image larger than 2^31 - 1 voxels (32-bit gather indices)");
+  }
+  // every call ends with a blocking read of the input maxima, which a
+  // capturing stream cannot take
+  {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(static_cast<cudaStream_t>(stream_ptr), &cs) != cudaSuccess ||
+        cs != cudaStreamCaptureStatusNone)
+      return fail(LC2_ERR_UNSUPPORTED,
+                  "lc2_evaluate_noalloc blocks on a read-back and cannot run on a capturing "
+                  "stream");
+  }
   for (int i = 0; i < (warp_nd == 2 ? 9 : 16); ++i)
     if (!std::isfinite(matrix[i])) return fail(LC2_ERR_INVALID_ARGUMENT, "non-finite transform");
 

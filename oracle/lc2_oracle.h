@@ -43,7 +43,7 @@ typedef struct {
 /* Reference zero threshold (src/cu_LC2/cu_lc2_helper.cuh:5). */
 #define OR_ZERO_THRESHOLD 1e-6
 
-/* Rank rule for the exact LS fit (documented in the design doc): a centred column
+/* Rank rule for the exact LS fit, shared with the GPU kernels: a centred column
  * whose sample variance is <= OR_DEGEN_VAR is dropped; two columns whose
  * squared correlation satisfies 1 - rho^2 <= OR_COLLINEAR are treated as one. */
 #define OR_DEGEN_VAR 1e-12

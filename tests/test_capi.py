@@ -94,3 +94,25 @@ def test_stack_rejects_bad_arguments_without_gpu():
     assert lib.lc2_stack_evaluate(None, 1, None, None, None) == 1
     assert lib.lc2_stack_frames(None) == 0
     assert lib.lc2_stack_destroy(None) == 0
+
+
+def test_noalloc_rejects_wrapping_sizes_without_gpu():
+    """lc2_evaluate_noalloc bounds the virtual grid axis by axis, so a grid
+    whose voxel count would wrap a 64-bit product (2^30 x 2^30 x 16) is
+    refused like any grid over LC2_NOALLOC_MAX_VOXELS, and so is a moving
+    image beyond 32-bit gather indices -- both before any device call."""
+    lib = capi.load()
+    dummy = ctypes.c_void_p(256)  # never dereferenced: the call fails first
+    m = (ctypes.c_float * 16)(*np.eye(4, dtype=np.float32).ravel())
+
+    def call(vdim, mdim):
+        v = capi._geom(Geometry(vdim, (1, 1, 1), (0, 0, 0)))
+        g = capi._geom(Geometry(mdim, (1, 1, 1), (0, 0, 0)))
+        return lib.lc2_evaluate_noalloc(1, ctypes.byref(v), ctypes.byref(g), 2, dummy, dummy, m,
+                                        dummy, None)
+
+    assert call((1 << 30, 1 << 30, 16), (8, 8, 8)) == 6
+    assert b"LC2_NOALLOC_MAX_VOXELS" in lib.lc2_last_error()
+    assert call((1 << 10, 1 << 10, 2), (8, 8, 8)) == 6
+    assert call((16, 16, 16), (65536, 65536, 2)) == 6
+    assert b"2^31" in lib.lc2_last_error()
