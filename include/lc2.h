@@ -86,6 +86,15 @@ int lc2_destroy(lc2_context* ctx);
  * uploads (src/Interpolator/interpolator.cu:276,315,459-473). */
 int lc2_set_images(lc2_context* ctx, const float* fixed_host, const float* moving_host);
 
+/* lc2_set_images for images that are already in device memory of the
+ * context's device (float32, same layout): the buffers the reference's
+ * LC2_{2D,3D}_class hold as thrust::device_vector and fill on the device
+ * (src/cu_LC2/cu_lc2_3d.cuh:75-89, src/cu_LC2/cu_lc2_2d.cuh:55-66). The
+ * inputs are read, not kept: later changes to them need another call.
+ * Host pointers are refused with LC2_ERR_INVALID_ARGUMENT. */
+int lc2_set_images_device(lc2_context* ctx, const float* fixed_device,
+                          const float* moving_device);
+
 /* The configuration the context was created with. */
 int lc2_get_config(const lc2_context* ctx, lc2_config* out);
 

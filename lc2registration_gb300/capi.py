@@ -51,6 +51,7 @@ EXPORTED = [
     "lc2_graph_launches", "lc2_autotune", "lc2_get_config", "lc2_weighting_map",
     "lc2_warp_affine_2d", "lc2_stack_register", "lc2_server_submit_stack",
     "lc2_server_poll_stack", "lc2_stack_set_option", "lc2_stack_get_option",
+    "lc2_set_images_device",
 ]
 
 ALGORITHMS = {"direct_l": 1, "bobyqa": 2, "nelder_mead": 3}
@@ -166,6 +167,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "lc2_create": ([ctypes.POINTER(lc2_config), ctypes.POINTER(vp)], ctypes.c_int),
         "lc2_destroy": ([vp], ctypes.c_int),
         "lc2_set_images": ([vp, _fp, _fp], ctypes.c_int),
+        "lc2_set_images_device": ([vp, vp, vp], ctypes.c_int),
         "lc2_virtual_dims": ([vp, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "lc2_evaluate": ([vp, _fp, _dp], ctypes.c_int),
         "lc2_evaluate_batch": ([vp, _fp, ctypes.c_int, _dp], ctypes.c_int),
@@ -328,6 +330,11 @@ class Context:
     def set_images(self, fixed: np.ndarray, moving: np.ndarray):
         f, m = _f32(fixed), _f32(moving)
         _check(self._lib.lc2_set_images(self._h, f.ctypes.data_as(_fp), m.ctypes.data_as(_fp)))
+
+    def set_images_device(self, fixed_ptr: int, moving_ptr: int):
+        """lc2_set_images from device pointers (float32 on the context's device)."""
+        _check(self._lib.lc2_set_images_device(self._h, ctypes.c_void_p(fixed_ptr),
+                                               ctypes.c_void_p(moving_ptr)))
 
     def virtual_dims(self):
         d = (ctypes.c_int * 3)()

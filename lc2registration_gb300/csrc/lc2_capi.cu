@@ -1112,8 +1112,37 @@ int image_absmax(const float* img, size_t n, const char* what, float* out) {
   return LC2_OK;
 }
 
-// Host float image -> device buffer of the storage type (synchronous).
-int upload_image(lc2_context* c, const float* host, size_t n, void* dst, int storage) {
+// Largest |value| of a device float image (as float bits, atomicMax on the
+// non-negative bit patterns orders them like the values) and a flag for
+// NaN/Inf anywhere in it. out[0] and out[1] must start at zero.
+__global__ void k_absmax_flag(const float* __restrict__ a, size_t n, unsigned int* __restrict__ out) {
+  unsigned int m = 0, bad = 0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const float v = a[i];
+    if (!isfinite(v)) bad = 1;
+    m = max(m, __float_as_uint(fabsf(v)));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+    bad |= __shfl_down_sync(0xffffffffu, bad, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(out, m);
+    if (bad) atomicOr(out + 1, 1u);
+  }
+}
+
+// Host float image -> device buffer of the storage type (synchronous). A
+// device-resident source (lc2_set_images_device) is converted in place of
+// the staging copy.
+int upload_image(lc2_context* c, const float* host, size_t n, void* dst, int storage,
+                 bool on_device = false) {
+  if (on_device) {
+    LC2_TRY(convert_to_storage(c, host, dst, n, storage));
+    LC2_CUDA(cudaStreamSynchronize(c->stream));
+    return LC2_OK;
+  }
   float* tmp = nullptr;
   LC2_CUDA(dev_alloc((void**)&tmp, sizeof(float) * n, c->stream));
   struct Free {
@@ -1269,7 +1298,9 @@ int set_fixed(lc2_context* c, const float* fixed, float fmax, float mmax) {
   float* ffix = nullptr;
   LC2_CUDA(dev_alloc((void**)&ffix, sizeof(float) * c->nf, c->stream));
   Free guard2{ffix, c->stream};
-  LC2_CUDA(cudaMemcpyAsync(ffix, fixed, sizeof(float) * c->nf, cudaMemcpyHostToDevice, c->stream));
+  // cudaMemcpyDefault: the fixed image is host memory (lc2_set_images) or
+  // device memory (lc2_set_images_device)
+  LC2_CUDA(cudaMemcpyAsync(ffix, fixed, sizeof(float) * c->nf, cudaMemcpyDefault, c->stream));
   lc2::Xform id{};
   {
     float ident[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
@@ -1376,6 +1407,43 @@ int lc2_set_images(lc2_context* c, const float* fixed, const float* moving) {
   LC2_TRY(image_absmax(moving, c->nm, "moving", &mmax));
   c->ready = false;
   LC2_TRY(upload_image(c, moving, c->nm, c->d_moving, c->cfg.storage));
+  return set_fixed(c, fixed, fmax, mmax);
+}
+
+int lc2_set_images_device(lc2_context* c, const float* fixed, const float* moving) {
+  g_err.clear();
+  if (!c || !fixed || !moving) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  if (!c->owns_moving)
+    return fail(LC2_ERR_INVALID_ARGUMENT, "the frames of a stack share the stack's moving volume");
+  LC2_TRY(select_device(c));
+  for (const float* p : {fixed, moving}) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess ||
+        (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) ||
+        at.device != c->cfg.device) {
+      cudaGetLastError();
+      return fail(LC2_ERR_INVALID_ARGUMENT,
+                  "lc2_set_images_device needs device memory of the context's device");
+    }
+  }
+  // largest |value| and NaN/Inf flag of each image, on the device
+  unsigned int* flags = reinterpret_cast<unsigned int*>(c->d_acc);  // 4 words, reset below
+  LC2_CUDA(cudaMemsetAsync(flags, 0, 4 * sizeof(unsigned int), c->stream));
+  const int blocks = 152 * 4;
+  k_absmax_flag<<<blocks, 256, 0, c->stream>>>(fixed, c->nf, flags);
+  k_absmax_flag<<<blocks, 256, 0, c->stream>>>(moving, c->nm, flags + 2);
+  LC2_CUDA(cudaGetLastError());
+  unsigned int h[4] = {0, 0, 0, 0};
+  LC2_CUDA(cudaMemcpyAsync(h, flags, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  LC2_CUDA(cudaStreamSynchronize(c->stream));
+  LC2_CUDA(cudaMemsetAsync(flags, 0, 4 * sizeof(unsigned int), c->stream));
+  if (h[1]) return fail(LC2_ERR_INVALID_ARGUMENT, "fixed image has NaN/Inf");
+  if (h[3]) return fail(LC2_ERR_INVALID_ARGUMENT, "moving image has NaN/Inf");
+  float fmax, mmax;
+  std::memcpy(&fmax, &h[0], 4);
+  std::memcpy(&mmax, &h[2], 4);
+  c->ready = false;
+  LC2_TRY(upload_image(c, moving, c->nm, c->d_moving, c->cfg.storage, true));
   return set_fixed(c, fixed, fmax, mmax);
 }
 
