@@ -240,12 +240,16 @@ int lc2_invert_affine_3d(const float in[16], float out[16]);
  * a non-zero return aborts with that status. Replaces the NLopt calls of
  * Optimizers{2D,3D,2DTo3D}::Optimize (src/Optimizers/optimizers.cu:298-302,
  * 385-390, 854-863, 937-946, 1473-1477, 1548-1553): LC2_OPT_DIRECT_L for
- * GN_ORIG_DIRECT_L, LC2_OPT_BOBYQA for LN_BOBYQA (a separable quadratic-model
- * trust region on 2n+1-point stencils; not Powell's update formulas),
- * LC2_OPT_NELDER_MEAD for LN_NELDERMEAD. xtol_rel is measured in units of
- * (upper - lower) per entry. */
+ * GN_ORIG_DIRECT_L, LC2_OPT_BOBYQA for LN_BOBYQA (Powell's 2009 method: 2n+1
+ * interpolation points, least-Frobenius-norm model updates, bounded
+ * trust-region and geometry steps; one evaluation per iteration after the
+ * first 2n+1, which come as one batch), LC2_OPT_NELDER_MEAD for
+ * LN_NELDERMEAD. LC2_OPT_QUAD_TR (no NLopt counterpart) is a batched
+ * separable quadratic-model trust region that evaluates a 2n+1-point stencil
+ * per step. xtol_rel (rho_end of BOBYQA) and initial_step (its rho_beg) are
+ * measured in units of (upper - lower) per entry. */
 typedef int (*lc2_batch_objective)(void* user, int count, int dim, const double* x, double* f);
-enum { LC2_OPT_DIRECT_L = 1, LC2_OPT_BOBYQA = 2, LC2_OPT_NELDER_MEAD = 3 };
+enum { LC2_OPT_DIRECT_L = 1, LC2_OPT_BOBYQA = 2, LC2_OPT_NELDER_MEAD = 3, LC2_OPT_QUAD_TR = 4 };
 typedef struct {
     int algorithm;        /* LC2_OPT_* */
     int dim;
@@ -286,7 +290,8 @@ typedef struct {
     int round_entries[8];  /* LC2_ENTRY_* mask per round; 0 = round disabled */
     double round_xtol[8];  /* the round's AbsTol */
     int round_maxeval;     /* per round; 0 = no limit */
-    int local_algorithm;   /* LC2_OPT_BOBYQA (default) or LC2_OPT_NELDER_MEAD */
+    int local_algorithm;   /* LC2_OPT_BOBYQA (default), LC2_OPT_NELDER_MEAD or
+                            * LC2_OPT_QUAD_TR */
     /* When lc2_register gets no context: LC2 of `count` matrices (row-major
      * 3x3 or 4x4 as doubles, dim = 9 or 16) from this callback instead, e.g.
      * a reference implementation for comparisons. */

@@ -54,7 +54,7 @@ EXPORTED = [
     "lc2_set_images_device",
 ]
 
-ALGORITHMS = {"direct_l": 1, "bobyqa": 2, "nelder_mead": 3}
+ALGORITHMS = {"direct_l": 1, "bobyqa": 2, "nelder_mead": 3, "quad_tr": 4}
 ENTRIES = {"translation": 1, "rotation": 2, "scale": 4, "shear": 8}
 
 OBSERVER = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,

@@ -12,7 +12,7 @@ def _quad(c, scale):
     return lambda X: (((X - c) * s) ** 2).sum(axis=1)
 
 
-@pytest.mark.parametrize("alg", ["bobyqa", "nelder_mead"])
+@pytest.mark.parametrize("alg", ["bobyqa", "nelder_mead", "quad_tr"])
 def test_local_methods_find_interior_minimum(alg):
     c = [1.5, -2.0, 0.25, 3.0, -0.7, 0.1]
     f = _quad(c, [1.0, 0.5, 4.0, 0.3, 2.0, 1.0])
@@ -23,11 +23,64 @@ def test_local_methods_find_interior_minimum(alg):
     assert batches < evals
 
 
-def test_trust_region_respects_bounds():
+@pytest.mark.parametrize("alg", ["bobyqa", "quad_tr"])
+def test_trust_region_respects_bounds(alg):
     f = _quad([10.0, -10.0, 0.0], [1, 1, 1])
     lo, hi = np.array([-1.0, -1.0, -1.0]), np.array([2.0, 3.0, 1.0])
-    x, fmin, _, _ = capi.minimize(f, [0.5, 0.5, 0.5], lo, hi, "bobyqa", xtol_rel=1e-8)
+    x, fmin, _, _ = capi.minimize(f, [0.5, 0.5, 0.5], lo, hi, alg, xtol_rel=1e-8)
     assert np.allclose(x, [2.0, -1.0, 0.0], atol=1e-5)
+
+
+# Standard test functions of derivative-free optimisation (the kind Powell
+# reports BOBYQA on): Rosenbrock, ARWHEAD, Powell's singular function, and a
+# scaled quadratic whose minimiser lies outside the box (bounds active).
+def _rosen(X):
+    return (100 * (X[:, 1:] - X[:, :-1] ** 2) ** 2 + (1 - X[:, :-1]) ** 2).sum(axis=1)
+
+
+def _arwhead(X):
+    return (((X[:, :-1] ** 2 + X[:, -1:] ** 2) ** 2) - 4 * X[:, :-1] + 3).sum(axis=1)
+
+
+def _powell_singular(X):
+    a, b, c, d = X.T
+    return (a + 10 * b) ** 2 + 5 * (c - d) ** 2 + (b - 2 * c) ** 4 + 10 * (a - d) ** 4
+
+
+@pytest.mark.parametrize("name,f,x0,lo,hi,xstar,fstar,tol,cap", [
+    ("rosenbrock2", _rosen, [-1.2, 1.0], -2.0, 2.0, [1.0, 1.0], 0.0, 1e-6, 400),
+    ("rosenbrock4", _rosen, [-1.2, 1.0, -1.2, 1.0], -2.0, 2.0, [1.0] * 4, 0.0, 1e-6, 900),
+    ("arwhead8", _arwhead, [1.0] * 8, -3.0, 3.0, [1.0] * 7 + [0.0], 0.0, 1e-5, 600),
+    ("powell_singular", _powell_singular, [3.0, -1.0, 0.0, 1.0], -2.0, 2.0, [0.0] * 4, 0.0,
+     2e-3, 1500),
+])
+def test_bobyqa_on_standard_test_functions(name, f, x0, lo, hi, xstar, fstar, tol, cap):
+    n = len(x0)
+    x, fmin, evals, batches = capi.minimize(f, np.array(x0, float), np.full(n, lo), np.full(n, hi),
+                                            "bobyqa", xtol_rel=1e-8, maxeval=5000,
+                                            initial_step=0.1)
+    assert np.abs(x - np.array(xstar)).max() < tol, (name, x)
+    assert fmin < fstar + 1e-9
+    assert evals <= cap, (name, evals)
+    # the 2n+1 initial points come as one batch, then one point per iteration
+    assert batches <= evals - 2 * n
+
+
+def test_bobyqa_active_bounds_and_quadratic_termination():
+    """A scaled quadratic whose minimiser lies outside the box: the optimum is
+    the projection, reached with the bounds active; a quadratic is modelled
+    exactly, so few evaluations are needed."""
+    n = 12
+    c = np.linspace(-1.0, 2.0, n)
+    s = np.linspace(0.5, 4.0, n)
+    f = lambda X: (((X - c) * s) ** 2).sum(axis=1)
+    x, fmin, evals, _ = capi.minimize(f, np.full(n, 0.5), np.zeros(n), np.ones(n), "bobyqa",
+                                      xtol_rel=1e-8, maxeval=2000, initial_step=0.1)
+    assert np.abs(x - np.clip(c, 0, 1)).max() < 1e-7
+    assert evals < 300
+    x, _, evals, _ = capi.minimize(f, np.zeros(n), np.full(n, -3.0), np.full(n, 3.0), "bobyqa",
+                                   xtol_rel=1e-8, maxeval=2000, initial_step=0.1)
+    assert np.abs(x - c).max() < 1e-6 and evals < 300
 
 
 def test_direct_finds_global_basin():
