@@ -69,10 +69,13 @@ def parse():
                     help="skip the HighResolutionModality: Fixed lines")
     ap.add_argument("--no-mi", action="store_true", help="skip the mutual-information lines")
     ap.add_argument("--no-bf16", action="store_true", help="skip the bf16-storage line")
+    ap.add_argument("--no-register", action="store_true",
+                    help="skip the registration (recovered-parameter) lines")
     ap.add_argument("--stack-frames", type=int, default=64)
     ap.add_argument("--stack-poses", type=int, default=256)
-    ap.add_argument("--serve-requests", type=int, default=48)
-    ap.add_argument("--serve-rate", type=float, default=4.0, help="Poisson arrivals per second")
+    ap.add_argument("--serve-requests", type=int, default=100, help="requests per offered rate")
+    ap.add_argument("--serve-rates", default="10,50,100,250,500",
+                    help="offered Poisson arrival rates (requests/s), comma-separated")
     ap.add_argument("--serve-active", type=int, default=8)
     return ap.parse_args()
 
@@ -209,7 +212,18 @@ def _registration(case, rng):
                         (["translation", "rotation", "scale", "shear"], 1e-6)])
 
 
-def serve_leg(args, main_case, device):
+def serve_sweep(args, main_case, device):
+    """The serving leg at each offered rate of --serve-rates (requests/s),
+    --serve-requests requests per rate."""
+    rates = [float(r) for r in str(args.serve_rates).split(",") if r.strip()]
+    rows = [serve_leg(args, main_case, device, rate, args.serve_requests) for rate in rates]
+    return {"rates": rows,
+            "note": "each rate: Poisson arrivals of the C5 mix on one server (merged launches "
+                    "for 2D and 2D-to-3D steps); above about 2 requests/s of 256^3 "
+                    "registrations the GPU is saturated and latency is queueing"}
+
+
+def serve_leg(args, main_case, device, rate, nreq):
     """Serving: Poisson arrivals of whole registrations, mix 40% 2D 256^2,
     30% 3D 128^3 -> 96^3, 20% 3D 256^3 FP16 (the main workload's volumes),
     10% 2D-to-3D stacks of 16 uneven frames cut from the 256^3 MR. Returns the
@@ -226,7 +240,7 @@ def serve_leg(args, main_case, device):
         "stack16": [synth.frame_stack(main_case.moving, main_case.moving_geom, 16, seed=105,
                                       spacing=0.5, r=3)],
     }
-    kinds = rng.choice(list(pools), size=args.serve_requests, p=[0.4, 0.3, 0.2, 0.1])
+    kinds = rng.choice(list(pools), size=nreq, p=[0.4, 0.3, 0.2, 0.1])
     srv = capi.Server(budget_bytes=0, max_active=args.serve_active, device=device)
 
     def submit(case, storage):
@@ -246,7 +260,7 @@ def serve_leg(args, main_case, device):
         else:
             tickets = [("one", submit(item, "f16" if k == "3d_256_f16" else "f32"))]
         sent.append((k, tickets))
-        time.sleep(rng.exponential(1.0 / args.serve_rate))
+        time.sleep(rng.exponential(1.0 / rate))
     lat = {k: [] for k in pools}
     queue = {k: [] for k in pools}
     run = {k: [] for k in pools}
@@ -269,7 +283,8 @@ def serve_leg(args, main_case, device):
     def pct(v, q):
         return float(np.percentile(v, q, method="inverted_cdf")) if len(v) else None
     return {
-        "requests": len(sent), "rate_offered": args.serve_rate,
+        "requests": len(sent), "rate_offered": rate,
+        "merged_launches": st["merged_launches"], "merged_steps": st["merged_steps"],
         "requests_per_s": len(sent) / wall, "evals_per_s": evals / wall,
         "p50_ms": pct(allv, 50), "p95_ms": pct(allv, 95), "p99_ms": pct(allv, 99),
         "by_kind_p50_ms": {k: pct(np.array(v), 50) for k, v in lat.items()},
@@ -574,6 +589,70 @@ def mi_leg(args, main_case, device):
     return out
 
 
+def registration_leg(args, device):
+    """Recovered parameters of the configured registrations, BOBYQA from the
+    identity: 2D 256^2 at most 200 evaluations, 3D 128^3 -> 96^3 at most 500;
+    each rigid (translation and rotation; scale and shear held at the
+    generating values) and affine (all 6 / 12 parameters). The GPU run is
+    timed end to end through lc2_register; the same driver with the FP64
+    oracle objective gives the reference parameters (skipped with --no-cpu)."""
+    import numpy as np
+
+    from lc2registration_gb300 import capi, synth
+    from tests.helpers import oracle_eval
+
+    out = {}
+    for cname, case, maxeval in (("2d_256", synth.case_2d(seed=7, size=256, r=3), 200),
+                                 ("3d_128_96", synth.case_3d(seed=8, mr_size=128, us_size=96,
+                                                             r=3), 500)):
+        p = case.true_params
+        if case.mode == "2D":
+            truth = np.array(list(p["trans"]) + [p["rot"]] + list(p["scale"]) + [p["shear"]])
+            nr = 3
+            lo_a, hi_a = [-12, -12, -10, 0.9, 0.9, -0.06], [12, 12, 10, 1.1, 1.1, 0.06]
+            init_a = [0, 0, 0, 1, 1, 0.0]
+        else:
+            truth = np.array(list(p["trans"]) + list(p["rot"]) + list(p["scale"]) +
+                             list(p["shear"]))
+            nr = 6
+            lo_a, hi_a = [-12] * 6 + [0.9] * 3 + [-0.05] * 3, [12] * 6 + [1.1] * 3 + [0.05] * 3
+            init_a = [0] * 6 + [1, 1, 1, 0, 0, 0.0]
+        init_r = np.concatenate([np.zeros(nr), truth[nr:]])
+        lo_r, hi_r = init_r.copy(), init_r.copy()
+        lo_r[:nr], hi_r[:nr] = -12.0, 12.0
+        for kind, init, lo, hi, entries in (
+                ("rigid", init_r, lo_r, hi_r, ["translation", "rotation"]),
+                ("affine", init_a, lo_a, hi_a, ["translation", "rotation", "scale", "shear"])):
+            kw = dict(center=case.fixed_geom.center(), direct_entries=[],
+                      rounds=[(entries, 1e-6)], round_maxeval=maxeval)
+            ctx = capi.Context(case.mode, case.fixed_geom, case.moving_geom, case.virt_spacing,
+                               case.r, True, "f32", device=device)
+            ctx.set_images(case.fixed, case.moving)
+            t0 = time.perf_counter()
+            gpu = capi.register(ctx, init, lo, hi, **kw)
+            wall = time.perf_counter() - t0
+            ctx.close()
+            err = np.abs(gpu["params"] - truth)
+            row = {"evaluations": gpu["evaluations"], "launches": gpu["launches"],
+                   "wall_ms": wall * 1e3, "lc2": gpu["lc2"],
+                   "max_err_vs_truth_mm_deg": float(err[:nr].max())}
+            if kind == "affine":
+                row["max_err_vs_truth_scale_shear"] = float(err[nr:].max())
+            if not args.no_cpu:
+                shape = (3, 3) if case.mode == "2D" else (4, 4)
+                orc = capi.register(None, init, lo, hi, mode=case.mode,
+                                    lc2_of_matrices=lambda M: np.array(
+                                        [oracle_eval(case, m.reshape(shape)) for m in M]), **kw)
+                d = np.abs(gpu["params"] - orc["params"])
+                row.update({"oracle_evaluations": orc["evaluations"], "oracle_lc2": orc["lc2"],
+                            "max_diff_vs_oracle_mm_deg": float(d[:nr].max()),
+                            "lc2_rel_diff_vs_oracle": abs(gpu["lc2"] / orc["lc2"] - 1.0)})
+                if kind == "affine":
+                    row["max_diff_vs_oracle_scale_shear"] = float(d[nr:].max())
+            out[f"{cname}_{kind}"] = row
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -772,12 +851,15 @@ def main():
     stack = None
     if rank == 0 and not args.no_stack:
         stack = stack_leg(args, case, local)
+    reg = None
+    if rank == 0 and not args.no_register:
+        reg = registration_leg(args, local)
     mi = None
     if rank == 0 and not args.no_mi:
         mi = mi_leg(args, case, local)
     serve = None
     if rank == 0 and not args.no_serve:
-        serve = serve_leg(args, case, local)
+        serve = serve_sweep(args, case, local)
 
     if rank == 0:
         line = {
@@ -805,6 +887,7 @@ def main():
             "fixed_modality": fixed,
             "stack": stack,
             "mutual_information": mi,
+            "registration": reg,
             "serve": serve,
             "gpu_launches": launches,
             "clocks": clk.summary(),

@@ -329,13 +329,22 @@ int lc2_params_to_matrix(int mode, const double* params, const float center[3],
  * and fewer than max_active are running; each admitted request runs on its
  * own worker thread with its own context and CUDA stream, so the kernels of
  * concurrent requests overlap on the GPU, and a request's images, weighting
- * factors and optimizer state stay resident until it completes. Results
- * are identical to the same request registered alone (lc2_register). */
+ * factors and optimizer state stay resident until it completes. The
+ * optimizer steps of concurrent 2D and 2D-to-3D requests are evaluated
+ * together in merged launches (merge_window_us). Results are identical to
+ * the same request registered alone (lc2_register). */
 typedef struct lc2_server lc2_server;
 typedef struct {
     size_t hbm_budget_bytes; /* device bytes admitted requests may hold; 0 = 80% of free memory */
     int max_active;          /* registrations in flight (worker threads); 0 = 8 */
     int device;              /* CUDA device of every request */
+    int merge_window_us;     /* cross-request batching of 2D and 2D-to-3D registrations
+                              * (HighResolutionModality Moving, PatchSize >= 1): the
+                              * optimizer steps of concurrent requests of one mode, patch
+                              * size and storage type are evaluated in one lc2_merger
+                              * launch; a step waits at most this long for the other
+                              * running requests' steps. 0 = 200 us, < 0 = off (each
+                              * request launches on its own stream). */
 } lc2_server_config;
 typedef struct {
     lc2_config config;       /* images, patch, storage (config.device is replaced by the server's) */
@@ -359,6 +368,8 @@ typedef struct {
     size_t budget_bytes, bytes_in_use, peak_bytes;
     double p50_ms, p95_ms, p99_ms, mean_ms; /* total latency of completed requests */
     double elapsed_s;                /* since creation or the last reset */
+    long long merged_launches;       /* merged launches since creation */
+    long long merged_steps;          /* optimizer steps they carried (one per request each) */
 } lc2_server_stats;
 
 /* A 2D-to-3D stack request: one moving volume, `frames` ultrasound frames
@@ -458,6 +469,26 @@ int lc2_stack_register(lc2_stack* s, int n, const int* frame_ids, const lc2_regi
 /* Kernel launches and graph launches issued by the stack since creation. */
 long long lc2_stack_launch_count(const lc2_stack* s);
 long long lc2_stack_graph_launches(const lc2_stack* s);
+
+/* ---- Cross-context batching ----
+ * Evaluations of several contexts -- e.g. the optimizer steps of concurrent
+ * registrations -- in one launch of the work-list kernel that 2D-to-3D stacks
+ * use (one segment per context, each with its own images, grid and
+ * fixed-point scales). The reference evaluates one transform of one
+ * registration per call (src/Optimizers/optimizers.cu:130-181); this has no
+ * counterpart there. Contexts must be 2D or 2D-to-3D, HighResolutionModality
+ * Moving, PatchSize >= 1, with images set, and share the mode, patch size,
+ * storage type and the merger's device. Values equal lc2_evaluate_batch on
+ * each context bit for bit. A merger is used by one host thread at a time. */
+typedef struct lc2_merger lc2_merger;
+int lc2_merger_create(int device, lc2_merger** out);
+int lc2_merger_destroy(lc2_merger* m);
+/* counts[i] transforms of ctxs[i]; matrices and lc2_out hold all of them in
+ * context order (3x3 in 2D mode, 4x4 in 2D-to-3D mode). */
+int lc2_merger_evaluate(lc2_merger* m, int n, lc2_context* const* ctxs, const int* counts,
+                        const float* matrices, double* lc2_out);
+/* Kernel launches issued by the merger since creation. */
+long long lc2_merger_launch_count(const lc2_merger* m);
 
 /* Evaluation for callers that cannot allocate device memory: a host
  * application whose allocator or memory pool owns the device heap, a

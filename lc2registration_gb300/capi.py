@@ -51,7 +51,8 @@ EXPORTED = [
     "lc2_graph_launches", "lc2_autotune", "lc2_get_config", "lc2_weighting_map",
     "lc2_warp_affine_2d", "lc2_stack_register", "lc2_server_submit_stack",
     "lc2_server_poll_stack", "lc2_stack_set_option", "lc2_stack_get_option",
-    "lc2_set_images_device",
+    "lc2_set_images_device", "lc2_merger_create", "lc2_merger_destroy", "lc2_merger_evaluate",
+    "lc2_merger_launch_count",
 ]
 
 ALGORITHMS = {"direct_l": 1, "bobyqa": 2, "nelder_mead": 3, "quad_tr": 4}
@@ -112,7 +113,7 @@ class lc2_config(ctypes.Structure):
 
 class lc2_server_config(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("max_active", ctypes.c_int),
-                ("device", ctypes.c_int)]
+                ("device", ctypes.c_int), ("merge_window_us", ctypes.c_int)]
 
 
 class lc2_request(ctypes.Structure):
@@ -143,7 +144,8 @@ class lc2_server_stats(ctypes.Structure):
                 ("bytes_in_use", ctypes.c_size_t), ("peak_bytes", ctypes.c_size_t),
                 ("p50_ms", ctypes.c_double), ("p95_ms", ctypes.c_double),
                 ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
-                ("elapsed_s", ctypes.c_double)]
+                ("elapsed_s", ctypes.c_double), ("merged_launches", ctypes.c_longlong),
+                ("merged_steps", ctypes.c_longlong)]
 
 
 _fp = ctypes.POINTER(ctypes.c_float)
@@ -168,6 +170,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "lc2_destroy": ([vp], ctypes.c_int),
         "lc2_set_images": ([vp, _fp, _fp], ctypes.c_int),
         "lc2_set_images_device": ([vp, vp, vp], ctypes.c_int),
+        "lc2_merger_create": ([ctypes.c_int, ctypes.POINTER(vp)], ctypes.c_int),
+        "lc2_merger_destroy": ([vp], ctypes.c_int),
+        "lc2_merger_evaluate": ([vp, ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_int),
+                                 _fp, _dp], ctypes.c_int),
+        "lc2_merger_launch_count": ([vp], ctypes.c_longlong),
         "lc2_virtual_dims": ([vp, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "lc2_evaluate": ([vp, _fp, _dp], ctypes.c_int),
         "lc2_evaluate_batch": ([vp, _fp, ctypes.c_int, _dp], ctypes.c_int),
@@ -445,6 +452,49 @@ class FrameView(Context):
 
     def close(self):
         self._h = ctypes.c_void_p()
+
+
+class Merger:
+    """lc2_merger_*: evaluations of several contexts in one launch."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load()
+        h = ctypes.c_void_p()
+        _check(self._lib.lc2_merger_create(int(device), ctypes.byref(h)))
+        self._h = h
+
+    def evaluate(self, contexts, mats_per_context):
+        """contexts: list of Context; mats_per_context: list of (count, 3|4, 3|4)
+        arrays. Returns a list of LC2 arrays, one per context."""
+        n = len(contexts)
+        counts = [len(m) for m in mats_per_context]
+        flat = np.ascontiguousarray(np.concatenate(
+            [np.asarray(m, dtype=np.float32).reshape(len(m), -1) for m in mats_per_context]),
+            dtype=np.float32)
+        out = np.empty(sum(counts), dtype=np.float64)
+        hs = (ctypes.c_void_p * n)(*[c.handle.value for c in contexts])
+        cs = (ctypes.c_int * n)(*counts)
+        _check(self._lib.lc2_merger_evaluate(self._h, n, hs, cs, flat.ctypes.data_as(_fp),
+                                             out.ctypes.data_as(_dp)))
+        res, k = [], 0
+        for c in counts:
+            res.append(out[k:k + c])
+            k += c
+        return res
+
+    def launch_count(self) -> int:
+        return int(self._lib.lc2_merger_launch_count(self._h))
+
+    def close(self):
+        if self._h:
+            self._lib.lc2_merger_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Stack:
@@ -730,11 +780,13 @@ class Server:
     """lc2_server_*: registrations admitted by device-memory budget, run
     concurrently on worker threads, results polled by ticket."""
 
-    def __init__(self, budget_bytes: int = 0, max_active: int = 0, device: int = 0):
+    def __init__(self, budget_bytes: int = 0, max_active: int = 0, device: int = 0,
+                 merge_window_us: int = 0):
         lib = load()
         self._lib = lib
         self._h = ctypes.c_void_p()
-        cfg = lc2_server_config(int(budget_bytes), int(max_active), int(device))
+        cfg = lc2_server_config(int(budget_bytes), int(max_active), int(device),
+                                int(merge_window_us))
         _check(lib.lc2_server_create(ctypes.byref(cfg), ctypes.byref(self._h)))
         self._keep = {}   # ticket -> callback objects the C side may still call
         self._errs = {}

@@ -1853,7 +1853,14 @@ struct lc2_stack {
   std::vector<Graph> graphs;
   bool use_graphs = true;
   bool batching = true;  // lc2_stack_register: lock-step merged launches
+  int wnd = 3;           // resampling dimensionality of the frames (2: 2D contexts)
   long long launches = 0, graph_launches = 0;
+};
+
+// Cross-context batching (lc2_merger_*): the stack's launch machinery without
+// a volume of its own; each segment names its context's moving image.
+struct lc2_merger {
+  lc2_stack s;
 };
 
 namespace {
@@ -1921,7 +1928,7 @@ int stack_enqueue(lc2_stack* s, int count, int nseg, long long units) {
   L.xf = s->d_xf;
   L.acc = s->d_acc;
   L.r = s->base.patch_size;
-  L.wnd = 3;
+  L.wnd = s->wnd;
   L.sms = s->sms;
   L.stream = st;
   cudaError_t e;
@@ -2207,6 +2214,127 @@ int lc2_stack_evaluate(lc2_stack* s, int count, const int* frame_ids, const floa
   for (int k = 0; k < count; ++k) lc2_out[order[k]] = s->h_out[k];
   return LC2_OK;
 }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Cross-context batching
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+int lc2_merger_create(int device, lc2_merger** out) {
+  g_err.clear();
+  if (!out) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  lc2_merger* m = new (std::nothrow) lc2_merger();
+  if (!m) return fail(LC2_ERR_OUT_OF_MEMORY, "host allocation failed");
+  lc2_stack* s = &m->s;
+  s->base.device = device;
+  s->base.high_res_is_moving = 1;
+  s->use_graphs = false;  // the segments change with the contexts of every call
+  int st = stack_select_device(s);
+  cudaError_t e = cudaSuccess;
+  if (st == LC2_OK) e = cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, device);
+  if (st == LC2_OK && e == cudaSuccess) {
+    int lo = 0, hi = 0;
+    e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    // the most urgent priority: merged launches carry small requests
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->stream, cudaStreamNonBlocking, hi);
+  }
+  if (st != LC2_OK || e != cudaSuccess) {
+    std::string msg = st != LC2_OK ? g_err : std::string(cudaGetErrorString(e));
+    lc2_merger_destroy(m);
+    return fail(st != LC2_OK ? st : LC2_ERR_CUDA, "merger: %s", msg.c_str());
+  }
+  *out = m;
+  return LC2_OK;
+}
+
+int lc2_merger_destroy(lc2_merger* m) {
+  if (!m) return LC2_OK;
+  lc2_stack* s = &m->s;
+  stack_select_device(s);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  stack_free_buffers(s);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete m;
+  return LC2_OK;
+}
+
+int lc2_merger_evaluate(lc2_merger* m, int n, lc2_context* const* ctxs, const int* counts,
+                        const float* matrices, double* lc2_out) {
+  g_err.clear();
+  if (!m || n < 0 || (n > 0 && (!ctxs || !counts))) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  lc2_stack* s = &m->s;
+  int total = 0, nseg = 0, mode = -1, r = -1, storage = -1;
+  for (int i = 0; i < n; ++i) {
+    const lc2_context* c = ctxs[i];
+    if (!c) return fail(LC2_ERR_INVALID_ARGUMENT, "context %d is null", i);
+    if (counts[i] < 0) return fail(LC2_ERR_INVALID_ARGUMENT, "negative count for context %d", i);
+    if (!c->ready) return fail(LC2_ERR_NOT_READY, "context %d: images not set", i);
+    if (c->lc2_nd != 2 || c->mi || !c->cfg.high_res_is_moving || c->generic)
+      return fail(LC2_ERR_UNSUPPORTED,
+                  "context %d: merged evaluation takes 2D and 2D-to-3D contexts with "
+                  "HighResolutionModality: Moving on the fused kernels", i);
+    if (c->cfg.device != s->base.device)
+      return fail(LC2_ERR_INVALID_ARGUMENT, "context %d is on device %d, the merger on %d", i,
+                  c->cfg.device, s->base.device);
+    if (mode < 0) {
+      mode = c->cfg.mode;
+      r = c->cfg.patch_size;
+      storage = c->cfg.storage;
+    } else if (c->cfg.mode != mode || c->cfg.patch_size != r || c->cfg.storage != storage) {
+      return fail(LC2_ERR_UNSUPPORTED,
+                  "merged contexts must share the mode, patch size and storage type");
+    }
+    total += counts[i];
+    if (counts[i] > 0) ++nseg;
+  }
+  if (total == 0) return LC2_OK;
+  if (!matrices || !lc2_out) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  const int mf = mode == LC2_MODE_2D ? 9 : 16;
+  for (int k = 0; k < total; ++k)
+    for (int i = 0; i < mf; ++i)
+      if (!std::isfinite(matrices[(size_t)k * mf + i]))
+        return fail(LC2_ERR_INVALID_ARGUMENT, "transform %d has NaN/Inf", k);
+  LC2_TRY(stack_select_device(s));
+  s->base.patch_size = r;
+  s->base.storage = storage;
+  s->wnd = mode == LC2_MODE_2D ? 2 : 3;
+  LC2_TRY(stack_capacity(s, total, nseg));
+  long long units = 0;
+  int k = 0, seg = 0;
+  for (int i = 0; i < n; ++i) {
+    if (counts[i] == 0) continue;
+    const lc2_context* c = ctxs[i];
+    lc2::ListSeg& S = s->h_segs[seg++];
+    S.mov = c->d_moving;
+    S.ust = c->d_static;
+    S.sig = c->d_sigma;
+    S.su = c->d_su;
+    S.P = c->fp;
+    S.P.ntx = (c->virt.dim[0] + 31) / 32;
+    S.P.zchunk = 1;
+    S.ntiles = S.P.ntx * ((c->virt.dim[1] + lc2::kListTY - 1) / lc2::kListTY);
+    S.count = counts[i];
+    S.eval0 = k;
+    S.pad_ = 0;
+    S.unit0 = units;
+    for (int e = 0; e < counts[i]; ++e, ++k) {
+      build_xform(c->warp_nd, c->virt, c->cfg.moving, matrices + (size_t)k * mf, &s->h_xf[k]);
+      s->h_sums[k] = c->sigma_sum;
+      units += S.ntiles;
+    }
+  }
+  LC2_TRY(stack_enqueue(s, total, nseg, units));
+  s->launches += 2;
+  LC2_CUDA(cudaStreamSynchronize(s->stream));
+  std::memcpy(lc2_out, s->h_out, sizeof(double) * total);
+  return LC2_OK;
+}
+
+long long lc2_merger_launch_count(const lc2_merger* m) { return m ? m->s.launches : 0; }
 
 }  // extern "C"
 

@@ -65,6 +65,107 @@ size_t image_voxels(const lc2_geometry& g, bool flat) {
   return (size_t)g.dim[0] * g.dim[1] * (flat ? 1 : g.dim[2]);
 }
 
+// Cross-request batching. Running requests of one mode, patch size and
+// storage type form a group; each optimizer step (the batch of transforms
+// lc2_register hands its objective) is queued in the group, and one thread --
+// the first to find no launch in progress -- takes every queued step, waits
+// up to the window for the steps of the group's other running requests,
+// evaluates them all in one lc2_merger launch and hands each request its
+// values. Steps that arrive during a launch go into the next one, so the
+// group's requests advance in merged rounds without a fixed batch. A merged
+// value equals the request's own lc2_evaluate_batch bit for bit, so every
+// registration follows the path it would follow alone.
+struct MergeStep {
+  lc2_context* ctx = nullptr;
+  int count = 0;
+  const float* mats = nullptr;
+  double* out = nullptr;
+  int status = LC2_OK;
+  std::string message;
+  bool done = false;
+};
+
+struct MergeGroup {
+  std::mutex mu;
+  std::condition_variable cv;
+  std::vector<MergeStep*> pending;
+  bool launching = false;
+  int members = 0;  // running requests of the group
+  lc2_merger* merger = nullptr;
+  long long launches = 0, steps = 0;
+  std::chrono::microseconds window{200};
+
+  int submit(MergeStep& step) {
+    std::unique_lock<std::mutex> lk(mu);
+    pending.push_back(&step);
+    cv.notify_all();
+    while (!step.done) {
+      if (launching) {
+        cv.wait(lk);
+        continue;
+      }
+      launching = true;
+      cv.wait_until(lk, Clock::now() + window, [&] { return (int)pending.size() >= members; });
+      std::vector<MergeStep*> take;
+      take.swap(pending);
+      lk.unlock();
+      std::vector<lc2_context*> ctxs;
+      std::vector<int> counts;
+      std::vector<float> mats;
+      size_t total = 0;
+      for (MergeStep* t : take) {
+        ctxs.push_back(t->ctx);
+        counts.push_back(t->count);
+        total += (size_t)t->count;
+      }
+      for (MergeStep* t : take) {
+        lc2_config c{};
+        lc2_get_config(t->ctx, &c);
+        const int f = c.mode == LC2_MODE_2D ? 9 : 16;
+        mats.insert(mats.end(), t->mats, t->mats + (size_t)t->count * f);
+      }
+      std::vector<double> out(total);
+      const int st = lc2_merger_evaluate(merger, (int)ctxs.size(), ctxs.data(), counts.data(),
+                                         mats.data(), out.data());
+      const std::string msg = st != LC2_OK ? lc2_last_error() : "";
+      lk.lock();
+      size_t k = 0;
+      for (MergeStep* t : take) {
+        if (st == LC2_OK) std::copy(out.begin() + k, out.begin() + k + t->count, t->out);
+        k += (size_t)t->count;
+        t->status = st;
+        t->message = msg;
+        t->done = true;
+      }
+      ++launches;
+      steps += (long long)take.size();
+      launching = false;
+      cv.notify_all();
+    }
+    if (step.status != LC2_OK) lc2_set_error_message(step.message.c_str());
+    return step.status;
+  }
+};
+
+// lc2_register's objective for a merged request: its matrices (exact float
+// values widened to double by the driver) go to the group as one step.
+struct MergeClient {
+  MergeGroup* group;
+  lc2_context* ctx;
+  std::vector<float> buf;
+};
+
+int merge_objective(void* user, int count, int dim, const double* m, double* f) {
+  MergeClient* mc = static_cast<MergeClient*>(user);
+  mc->buf.assign(m, m + (size_t)count * dim);
+  MergeStep step;
+  step.ctx = mc->ctx;
+  step.count = count;
+  step.mats = mc->buf.data();
+  step.out = f;
+  return mc->group->submit(step);
+}
+
 }  // namespace
 
 struct lc2_server {
@@ -144,7 +245,26 @@ struct lc2_server {
           (long long)vd[0] * vd[1] * vd[2] <= (1LL << 20))
         st = lc2_set_option(c, LC2_OPTION_STREAM_PRIORITY, -1000);
       if (st == LC2_OK) st = lc2_set_images(c, j.fixed.data(), j.moving.data());
-      if (st == LC2_OK) st = lc2_register(c, &reg, &out);
+      MergeGroup* g = nullptr;
+      if (st == LC2_OK) g = merge_group(cfg);
+      if (st == LC2_OK && g) {
+        MergeClient mc{g, c, {}};
+        lc2_registration merged = reg;
+        merged.lc2_of_matrices = merge_objective;
+        merged.user = &mc;
+        {
+          std::lock_guard<std::mutex> lk(g->mu);
+          ++g->members;
+        }
+        st = lc2_register(nullptr, &merged, &out);
+        {
+          std::lock_guard<std::mutex> lk(g->mu);
+          --g->members;
+        }
+        g->cv.notify_all();
+      } else if (st == LC2_OK) {
+        st = lc2_register(c, &reg, &out);
+      }
       std::string msg = st != LC2_OK ? lc2_last_error() : "";
       if (c) lc2_destroy(c);
       if (st != LC2_OK) lc2_set_error_message(msg.c_str());
@@ -152,6 +272,42 @@ struct lc2_server {
     j.res.status = st;
     j.res.result = out;
     if (st != LC2_OK) std::snprintf(j.res.message, sizeof(j.res.message), "%s", lc2_last_error());
+  }
+
+  // The merge group of a request's configuration, or nullptr where its steps
+  // are not merged (3D grids, HighResolutionModality Fixed, mutual
+  // information, merging off).
+  std::mutex merge_mu;
+  std::map<long long, std::unique_ptr<MergeGroup>> groups;
+  MergeGroup* merge_group(const lc2_config& c) {
+    if (cfg.merge_window_us < 0 || c.mode == LC2_MODE_3D || !c.high_res_is_moving ||
+        c.patch_size < 1)
+      return nullptr;
+    const long long key = ((long long)c.mode * 64 + c.patch_size) * 8 + c.storage;
+    std::lock_guard<std::mutex> lk(merge_mu);
+    auto& g = groups[key];
+    if (!g) {
+      std::unique_ptr<MergeGroup> ng(new MergeGroup());
+      ng->window = std::chrono::microseconds(cfg.merge_window_us > 0 ? cfg.merge_window_us : 200);
+      if (lc2_merger_create(cfg.device, &ng->merger) != LC2_OK) {
+        groups.erase(key);
+        return nullptr;
+      }
+      g = std::move(ng);
+    }
+    return g.get();
+  }
+  void merge_counts(long long* launches, long long* steps) {
+    std::lock_guard<std::mutex> lk(merge_mu);
+    *launches = *steps = 0;
+    for (auto& kv : groups) {
+      std::lock_guard<std::mutex> gl(kv.second->mu);
+      *launches += kv.second->launches;
+      *steps += kv.second->steps;
+    }
+  }
+  ~lc2_server() {
+    for (auto& kv : groups) lc2_merger_destroy(kv.second->merger);
   }
 
   void worker() {
@@ -394,6 +550,7 @@ int lc2_server_get_stats(lc2_server* s, lc2_server_stats* out) {
   out->bytes_in_use = s->used;
   out->peak_bytes = s->peak;
   out->elapsed_s = std::chrono::duration<double>(Clock::now() - s->t0).count();
+  s->merge_counts(&out->merged_launches, &out->merged_steps);
   if (!s->latencies.empty()) {
     std::vector<double> v = s->latencies;
     std::sort(v.begin(), v.end());

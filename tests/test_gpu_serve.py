@@ -98,3 +98,49 @@ def test_stack_request_equals_stack_registration():
     with pytest.raises(capi.LC2Error, match="unknown"):
         srv.poll_stack(t)
     srv.close()
+
+
+def test_merger_equals_each_context_alone():
+    """lc2_merger_evaluate: transforms of 2D contexts of different sizes (and,
+    separately, 2D-to-3D frames of different sizes with their own volumes) in
+    one launch give each context's own lc2_evaluate_batch values bit for bit."""
+    rng = np.random.default_rng(8)
+    m = capi.Merger()
+    cases = [synth.case_2d(seed=s, size=sz, r=3) for s, sz in ((31, 64), (32, 96), (33, 72))]
+    for group in (cases, None):
+        if group is None:
+            group = []
+            for s, sides in ((34, (40,)), (35, (56,))):
+                mr = synth.mr_phantom((40, 40, 40), 6, 1.5, seed=s)
+                mg = Geometry((40, 40, 40), (1.0, 1.0, 1.0), (0.0, 0.0, 0.0))
+                group += synth.frame_stack(mr, mg, 1, seed=s + 1, sides=sides, spacing=0.5, r=3)
+        ctxs = [make_context(c) for c in group]
+        from tests.helpers import perturbed
+        mats = [perturbed(c, rng, k) for c, k in zip(group, (5, 1, 3)[:len(group)])]
+        got = m.evaluate(ctxs, mats)
+        for c, mm, g in zip(ctxs, mats, got):
+            np.testing.assert_array_equal(g, c.evaluate_batch(mm))
+    assert m.launch_count() == 4  # list kernel + ratio per merged call
+    m.close()
+
+
+def test_concurrent_2d_requests_share_launches():
+    """Six 2D registrations running at once: their optimizer steps are merged
+    into shared launches, and each result equals the registration alone."""
+    cases = [synth.case_2d(seed=s, size=sz, r=3) for s, sz in
+             ((41, 64), (42, 80), (43, 64), (44, 96), (45, 72), (46, 64))]
+    alone = [capi.register(make_context(c), **_reg(c)) for c in cases]
+    srv = capi.Server(budget_bytes=2 << 30, max_active=len(cases), merge_window_us=2000)
+    tickets = []
+    for c in cases:
+        cfg = capi.make_config(c.mode, c.fixed_geom, c.moving_geom, c.virt_spacing, c.r, True)
+        tickets.append(srv.submit(cfg, c.fixed, c.moving, **_reg(c)))
+    for t, a in zip(tickets, alone):
+        r = srv.poll(t)
+        assert r["status"] == 0, r["message"]
+        np.testing.assert_array_equal(r["params"][:6], a["params"])
+        assert r["lc2"] == a["lc2"] and r["evaluations"] == a["evaluations"]
+    st = srv.stats()
+    assert st["merged_launches"] > 0
+    assert st["merged_steps"] > 1.5 * st["merged_launches"], st
+    srv.close()
