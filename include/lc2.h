@@ -196,6 +196,15 @@ enum { LC2_OPTION_STREAM_PRIORITY = 5 };
  * The values agree to FP32 resampling rounding (the two paths place their
  * sampling bases differently). */
 enum { LC2_OPTION_GENERIC = 7 };
+/* LC2_OPTION_PRESAMPLE (3D, HighResolutionModality Moving): 1 runs the
+ * resampling of the moving image as a pass of its own -- one float per
+ * virtual voxel and transform, written to a context buffer of at most 4 GiB
+ * (64 transforms at 256^3; larger batches go in groups) -- and the fused
+ * kernel reads it instead of gathering; 0 resamples inside the fused kernel.
+ * Each voxel is sampled once from its 32 x 8 tile's base in the first form,
+ * from its fused tile's base in the second, so the two agree to FP32
+ * resampling rounding, not bit for bit. */
+enum { LC2_OPTION_PRESAMPLE = 8 };
 int lc2_set_option(lc2_context* ctx, int option, int value);
 
 /* CUDA-graph launches issued by lc2_evaluate_batch / lc2_evaluate. */

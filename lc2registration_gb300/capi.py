@@ -33,6 +33,7 @@ OPTION_PIPELINE = 4
 OPTION_STREAM_PRIORITY = 5
 OPTION_STACK_BATCHING = 6
 OPTION_GENERIC = 7
+OPTION_PRESAMPLE = 8
 STORAGE = {"f32": 0, "f16": 1, "bf16": 2}
 
 # Every symbol include/lc2.h declares (checked by the test suite).

@@ -178,6 +178,9 @@ struct lc2_context {
   int tile_rows = 0;  // fused kernel tile height (0 = automatic)
   int zchunk = 0;     // fused kernel output slices per CTA (0 = automatic)
   int pipeline = 0;   // warp-specialised fused 3D kernel (LC2_OPTION_PIPELINE)
+  int presample = 0;  // 3D: resample as a pass of its own (LC2_OPTION_PRESAMPLE)
+  float* d_pre = nullptr;  // presampled moving image, pre_slots transforms
+  int pre_slots = 0;
   int* d_err = nullptr;   // device flag of the warp-specialised kernel's bounded waits
   int* h_err = nullptr;   // pinned copy
 
@@ -581,6 +584,22 @@ int tile_rows(const lc2_context* c) {
 }
 
 // The fused kernel (static ultrasound): one launch for `cnt` transforms.
+// Transforms per presample group: the buffer holds at most 4 GiB (64
+// transforms of a 256^3 grid), at most 64 transforms.
+constexpr size_t kPresampleBytes = size_t(4) << 30;
+int presample_slots(const lc2_context* c) {
+  const size_t per = sizeof(float) * c->nv;
+  return (int)std::max<size_t>(1, std::min<size_t>(64, kPresampleBytes / per));
+}
+
+int ensure_presample(lc2_context* c) {
+  if (c->d_pre) return LC2_OK;
+  const int slots = presample_slots(c);
+  LC2_CUDA(dev_alloc((void**)&c->d_pre, sizeof(float) * c->nv * (size_t)slots, c->stream));
+  c->pre_slots = slots;
+  return LC2_OK;
+}
+
 int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
   c->acc_clean = false;
   if (!c->cfg.high_res_is_moving || !c->d_sigma || !c->d_su)
@@ -610,15 +629,45 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
   L.err = c->d_err;
   L.sms = c->sms;
   L.stream = c->stream;
+  auto fused = [&]() {
+    if (c->cfg.storage == LC2_STORE_F16) return lc2::fused_launch<__half>(L);
+    if (c->cfg.storage == LC2_STORE_BF16) return lc2::fused_launch<__nv_bfloat16>(L);
+    return lc2::fused_launch<float>(L);
+  };
   cudaError_t e;
+  if (c->presample && c->lc2_nd == 3 && !c->pipeline) {
+    // resample pass, then the fused kernel on the presampled images, in
+    // groups of the presample buffer's capacity
+    LC2_TRY(ensure_presample(c));
+    for (int j = 0; j < cnt; j += c->pre_slots) {
+      const int n = std::min(c->pre_slots, cnt - j);
+      {
+        TimerScope ts(c, K_WARP);
+        if (c->cfg.storage == LC2_STORE_F16)
+          e = lc2::presample_launch<__half>(c->d_moving, c->fp, c->d_xf, k0 + j, n, c->d_pre, c->stream);
+        else if (c->cfg.storage == LC2_STORE_BF16)
+          e = lc2::presample_launch<__nv_bfloat16>(c->d_moving, c->fp, c->d_xf, k0 + j, n, c->d_pre,
+                                                   c->stream);
+        else
+          e = lc2::presample_launch<float>(c->d_moving, c->fp, c->d_xf, k0 + j, n, c->d_pre, c->stream);
+      }
+      ++c->launches;
+      LC2_CUDA(e);
+      L.k0 = k0 + j;
+      L.cnt = n;
+      L.pre = c->d_pre;
+      {
+        TimerScope ts(c, K_MOMENTS);
+        e = fused();
+      }
+      ++c->launches;
+      LC2_CUDA(e);
+    }
+    return LC2_OK;
+  }
   {
     TimerScope ts(c, K_MOMENTS);
-    if (c->cfg.storage == LC2_STORE_F16)
-      e = lc2::fused_launch<__half>(L);
-    else if (c->cfg.storage == LC2_STORE_BF16)
-      e = lc2::fused_launch<__nv_bfloat16>(L);
-    else
-      e = lc2::fused_launch<float>(L);
+    e = fused();
   }
   ++c->launches;
   LC2_CUDA(e);
@@ -953,6 +1002,7 @@ int lc2_destroy(lc2_context* c) {
   dev_free(c->d_gstatic, fs);
   dev_free(c->d_sigma, fs);
   dev_free(c->d_su, fs);
+  dev_free(c->d_pre, fs);
   dev_free(c->d_fq, fs);
   dev_free(c->d_fs, fs);
   dev_free(c->d_fd, fs);
@@ -1047,6 +1097,15 @@ int lc2_set_option(lc2_context* c, int option, int value) {
   }
   if (option == LC2_OPTION_PIPELINE) {
     c->pipeline = value != 0;
+    drop_graphs(c);
+    return LC2_OK;
+  }
+  if (option == LC2_OPTION_PRESAMPLE) {
+    if (value != 0 && value != 1) return fail(LC2_ERR_INVALID_ARGUMENT, "presample must be 0 or 1");
+    if (value == 1 && (c->lc2_nd != 3 || !c->cfg.high_res_is_moving || c->mi))
+      return fail(LC2_ERR_UNSUPPORTED, "presampling exists for 3D LC2 contexts with "
+                  "HighResolutionModality: Moving");
+    c->presample = value;
     drop_graphs(c);
     return LC2_OK;
   }

@@ -560,11 +560,47 @@ constexpr int fused_min_blocks(int nd, int ty, int r) {
   return nd == 2 ? (ty == 32 ? 2 : 4) : (ty == 8 && r <= 4 ? 2 : 1);
 }
 
-template <int ND, int WND, typename TM, typename TS, int TY, int R>
+// Resample stage as a pass of its own (presampling): the moving image on the
+// virtual grid for `count` transforms, one float per voxel, slot-major. Each
+// 32 x 8 tile slice samples from its own base (tile_base, as the generic
+// resampling kernel does), so every voxel has one value whichever fused CTA
+// reads it; slices that sample strictly inside the moving image skip the
+// bounds tests (same bits).
+template <typename TM>
+__global__ void __launch_bounds__(256) k_presample(const TM* __restrict__ mov, int mx, int my,
+                                                   int mz, int vx, int vy,
+                                                   const Xform* __restrict__ xf, int k0,
+                                                   float* __restrict__ out) {
+  __shared__ TileBase T;
+  __shared__ int s_in;
+  const int ntx = (vx + 31) >> 5;
+  const int x0 = (blockIdx.x % ntx) * 32, y0 = (blockIdx.x / ntx) * 8;
+  const int z = blockIdx.y, slot = blockIdx.z;
+  const int tid = threadIdx.x;
+  const Xform* X = xf + k0 + slot;
+  if (tid < 3) xform_coord(*X, tid, x0, y0, z, T.ib[tid], T.fb[tid]);
+  if (tid < 9) T.A[tid] = X->ah[tid];
+  __syncthreads();
+  if (tid == 0) s_in = tile_inside(T, mx, my, mz) ? 1 : 0;
+  __syncthreads();
+  const int tx = tid & 31, ty = tid >> 5;
+  const int x = x0 + tx, y = y0 + ty;
+  if (x >= vx || y >= vy) return;
+  const float v = s_in ? tile_sample_inside<TM>(mov, mx, my, T, tx, ty)
+                       : tile_sample<3, TM>(mov, mx, my, mz, T, tx, ty);
+  const size_t nv = (size_t)vx * vy * gridDim.y;
+  out[(size_t)slot * nv + ((size_t)z * vy + y) * vx + x] = v;
+}
+
+// PRE: the moving image is read from a presampled buffer (k_presample, one
+// float per virtual voxel and transform of the launch, slot-major) instead of
+// being resampled by the CTA.
+template <int ND, int WND, typename TM, typename TS, int TY, int R, bool PRE = false>
 __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
     k_fused(const TM* __restrict__ mov, const TS* __restrict__ Ust, const float* __restrict__ sig,
             const int* __restrict__ su, FusedParams P, const Xform* __restrict__ xf, int k0,
-            unsigned long long* __restrict__ acc, float* __restrict__ out_measure) {
+            unsigned long long* __restrict__ acc, float* __restrict__ out_measure,
+            const float* __restrict__ pre = nullptr) {
   using G = FusedGeom<ND, TY, R>;
   constexpr int NT = G::NT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -596,6 +632,7 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
   // fraction for the float per-point offsets; run by the last thread, whose
   // warp holds the fewest halo points
   auto set_base = [&](int zs) {
+    if (PRE) return;
     if (tid == NT - 1)
       s_inside = region_base<3, G::PW, G::PH>(s_xf, s_A, P, gx0, gy0, yb, zs,
                                               ND == 3 && zs >= 0 && zs < P.vz, s_ib, s_fb)
@@ -661,6 +698,20 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
       pu[j] = pin[j] ? gy * P.vx + gx : 0;
     }
     const size_t slice = (size_t)P.vx * P.vy;
+    // presampled input: this transform's images and the in-slice offset of
+    // each of the thread's region points (-1 outside the grid: zero padding)
+    const float* pre_slot = PRE ? pre + (size_t)slot * slice * P.vz : nullptr;
+    int poff[PRE ? WP : 1];
+    if constexpr (PRE) {
+#pragma unroll
+      for (int k = 0; k < WP; ++k) {
+        const int i = tid + k * NT;
+        const int py = i / G::PW, px = i - py * G::PW;
+        const int gx = gx0 + px, gy = gy0 + py;
+        poff[k] = (i < G::NPW && gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy) ? gy * P.vx + gx
+                                                                                : -1;
+      }
+    }
     float m_prev2[WP], m_prev1[WP];  // M of the thread's region points, slices e-1, e
     const int e0 = zb - R;           // first slice entering the window
     // static ultrasound of the entering and leaving slices, loaded one
@@ -694,6 +745,12 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
     load_sig(e0 - R);
     auto warp_slice = [&](int zs, float* out) {
       const bool zin = (zs >= 0 && zs < P.vz);
+      if constexpr (PRE) {
+        const float* src = pre_slot + (size_t)(zin ? zs : 0) * ((size_t)P.vx * P.vy);
+#pragma unroll
+        for (int k = 0; k < WP; ++k) out[k] = (zin && poff[k] >= 0) ? __ldg(src + poff[k]) : 0.0f;
+        return;
+      }
       if (s_inside) {
 #pragma unroll
         for (int k = 0; k < WP; ++k) {
@@ -731,11 +788,21 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
     __syncthreads();
     set_base(e0 + 1);
     __syncthreads();
+    // presampled input: slice e+1 is loaded during iteration e-1, so its
+    // global-memory latency overlaps a whole iteration
+    float m_pf[PRE ? WP : 1];
+    if constexpr (PRE) warp_slice(e0 + 1, m_pf);
     for (int e = e0; e < ze + R; ++e) {
       // resample slice e+1; write the planes of slice e
       {
         float m_next[WP];
-        warp_slice(e + 1, m_next);
+        if constexpr (PRE) {
+#pragma unroll
+          for (int k = 0; k < WP; ++k) m_next[k] = m_pf[k];
+          warp_slice(e + 2, m_pf);
+        } else {
+          warp_slice(e + 1, m_next);
+        }
 #pragma unroll
         for (int k = 0; k < WP; ++k) {
           const int i = tid + k * NT;
@@ -854,14 +921,25 @@ struct FusedLaunch {
   int* err;         // device flag raised by the warp-specialised kernel's bounded waits
   int sms;          // multiprocessors of the device
   cudaStream_t stream;
+  const float* pre = nullptr;  // 3D: presampled moving image of the launch (k_presample)
 };
+
+template <int ND, int WND, typename T, int R, int TY, typename K>
+cudaError_t fused_launch_grid(const FusedLaunch& L, K kern);
 
 template <int ND, int WND, typename T, int R, int TY>
 cudaError_t fused_launch_rt(const FusedLaunch& L) {
-  using G = FusedGeom<ND, TY, R>;
   if (L.P.kbits != PatchConst<ND, R>::K || L.P.n != PatchConst<ND, R>::N)
     return cudaErrorInvalidValue;
-  auto kern = k_fused<ND, WND, T, T, TY, R>;
+  if constexpr (ND == 3) {
+    if (L.pre) return fused_launch_grid<ND, WND, T, R, TY>(L, k_fused<ND, WND, T, T, TY, R, true>);
+  }
+  return fused_launch_grid<ND, WND, T, R, TY>(L, k_fused<ND, WND, T, T, TY, R, false>);
+}
+
+template <int ND, int WND, typename T, int R, int TY, typename K>
+cudaError_t fused_launch_grid(const FusedLaunch& L, K kern) {
+  using G = FusedGeom<ND, TY, R>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)G::BYTES);
   if (e != cudaSuccess) return e;
@@ -881,7 +959,18 @@ cudaError_t fused_launch_rt(const FusedLaunch& L) {
   }
   dim3 grid(L.cnt, ntx * nty, nz);
   kern<<<grid, G::NT, G::BYTES, L.stream>>>((const T*)L.mov, (const T*)L.ust, L.sig, L.su, P, L.xf,
-                                             L.k0, L.acc, L.out_measure);
+                                             L.k0, L.acc, L.out_measure, L.pre);
+  return cudaGetLastError();
+}
+
+// k_presample of transforms [k0, k0 + cnt) into pre (cnt x voxels floats).
+template <typename T>
+cudaError_t presample_launch(const void* mov, const FusedParams& P, const Xform* xf, int k0,
+                             int cnt, float* pre, cudaStream_t stream) {
+  const int ntx = (P.vx + 31) / 32, nty = (P.vy + 7) / 8;
+  dim3 grid(ntx * nty, P.vz, cnt);
+  k_presample<T><<<grid, 256, 0, stream>>>((const T*)mov, P.mx, P.my, P.mz, P.vx, P.vy, xf, k0,
+                                           pre);
   return cudaGetLastError();
 }
 
