@@ -531,6 +531,15 @@ int lc2_evaluate_noalloc(int mode, const lc2_geometry* virt, const lc2_geometry*
                          int patch_size, const float* d_ultrasound, const float* d_moving,
                          const float* matrix, double* d_lc2, void* stream);
 
+/* Test hooks for the failure paths (no counterpart in the reference, which
+ * checks no allocation). lc2_debug_fail_allocation(k): the k-th device or
+ * pinned-host allocation the library makes from now on (any thread) fails
+ * as an out-of-memory would, without calling CUDA; k = 0 disarms it.
+ * lc2_debug_device_bytes: device bytes and allocations the library holds
+ * now, to check that a failed call released what it had taken. */
+int lc2_debug_fail_allocation(long long k);
+int lc2_debug_device_bytes(size_t* live_bytes, long long* live_allocations);
+
 /* Message of the last failure on the calling thread ("" if none). */
 const char* lc2_last_error(void);
 

@@ -53,7 +53,7 @@ EXPORTED = [
     "lc2_warp_affine_2d", "lc2_stack_register", "lc2_server_submit_stack",
     "lc2_server_poll_stack", "lc2_stack_set_option", "lc2_stack_get_option",
     "lc2_set_images_device", "lc2_merger_create", "lc2_merger_destroy", "lc2_merger_evaluate",
-    "lc2_merger_launch_count",
+    "lc2_merger_launch_count", "lc2_debug_fail_allocation", "lc2_debug_device_bytes",
 ]
 
 ALGORITHMS = {"direct_l": 1, "bobyqa": 2, "nelder_mead": 3, "quad_tr": 4}
@@ -176,6 +176,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "lc2_merger_evaluate": ([vp, ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_int),
                                  _fp, _dp], ctypes.c_int),
         "lc2_merger_launch_count": ([vp], ctypes.c_longlong),
+        "lc2_debug_fail_allocation": ([ctypes.c_longlong], ctypes.c_int),
+        "lc2_debug_device_bytes": ([ctypes.POINTER(ctypes.c_size_t),
+                                    ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
         "lc2_virtual_dims": ([vp, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "lc2_evaluate": ([vp, _fp, _dp], ctypes.c_int),
         "lc2_evaluate_batch": ([vp, _fp, ctypes.c_int, _dp], ctypes.c_int),

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <atomic>
 #include <cstring>
 #include <limits>
 #include <map>
@@ -57,7 +58,27 @@ size_t elem_size(int storage) { return storage == LC2_STORE_F32 ? 4 : 2; }
 // keep what is freed (release threshold: unlimited), so creating and
 // destroying contexts never synchronises the device: cudaFree would wait for
 // every stream, i.e. for other requests' kernels.
+// Allocation-failure injection (lc2_debug_fail_allocation) and the account of
+// live device bytes it is checked against. Test hooks on the host: a failed
+// allocation returns cudaErrorMemoryAllocation without calling CUDA.
+std::atomic<long long> g_fail_countdown{0};
+std::mutex g_live_mu;
+std::map<void*, size_t> g_live;
+size_t g_live_bytes = 0;
+
+bool injected_failure() {
+  long long k = g_fail_countdown.load();
+  while (k > 0) {
+    if (g_fail_countdown.compare_exchange_weak(k, k - 1)) return k == 1;
+  }
+  return false;
+}
+
 cudaError_t dev_alloc(void** p, size_t n, cudaStream_t st) {
+  if (n > 0 && injected_failure()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
   static std::mutex mu;
   static std::vector<int> ready;
   int dev = 0;
@@ -77,11 +98,26 @@ cudaError_t dev_alloc(void** p, size_t n, cudaStream_t st) {
   }
   *p = nullptr;
   if (n == 0) return cudaSuccess;
-  return cudaMallocAsync(p, n, st);
+  e = cudaMallocAsync(p, n, st);
+  if (e == cudaSuccess) {
+    std::lock_guard<std::mutex> lk(g_live_mu);
+    g_live[*p] = n;
+    g_live_bytes += n;
+  }
+  return e;
 }
 
 void dev_free(void* p, cudaStream_t st) {
-  if (p) cudaFreeAsync(p, st);
+  if (!p) return;
+  {
+    std::lock_guard<std::mutex> lk(g_live_mu);
+    auto it = g_live.find(p);
+    if (it != g_live.end()) {
+      g_live_bytes -= it->second;
+      g_live.erase(it);
+    }
+  }
+  cudaFreeAsync(p, st);
 }
 
 // Pinned host buffers are cached by power-of-two size and reused (cudaFreeHost
@@ -91,6 +127,10 @@ std::multimap<size_t, void*> g_pin_free;
 std::map<void*, size_t> g_pin_size;
 
 cudaError_t host_alloc(void** p, size_t n) {
+  if (injected_failure()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
   size_t cls = 4096;
   while (cls < n) cls <<= 1;
   {
@@ -1050,6 +1090,19 @@ int lc2_set_stream(lc2_context* c, void* stream) {
 }
 
 long long lc2_launch_count(const lc2_context* c) { return c ? c->launches : 0; }
+
+int lc2_debug_fail_allocation(long long k) {
+  g_fail_countdown.store(k > 0 ? k : 0);
+  return LC2_OK;
+}
+
+int lc2_debug_device_bytes(size_t* live_bytes, long long* live_allocations) {
+  if (!live_bytes || !live_allocations) return fail(LC2_ERR_INVALID_ARGUMENT, "null argument");
+  std::lock_guard<std::mutex> lk(g_live_mu);
+  *live_bytes = g_live_bytes;
+  *live_allocations = (long long)g_live.size();
+  return LC2_OK;
+}
 
 int lc2_set_option(lc2_context* c, int option, int value) {
   if (!c) return fail(LC2_ERR_INVALID_ARGUMENT, "null context");
