@@ -565,31 +565,68 @@ constexpr int fused_min_blocks(int nd, int ty, int r) {
 // 32 x 8 tile slice samples from its own base (tile_base, as the generic
 // resampling kernel does), so every voxel has one value whichever fused CTA
 // reads it; slices that sample strictly inside the moving image skip the
-// bounds tests (same bits).
+// bounds tests (same bits). A CTA covers kPreZ slices of one tile: their
+// bases are computed by 3 kPreZ threads at once, and each thread then has
+// kPreZ independent samples in flight. The output is written with streaming
+// stores (it is read once, by another kernel, and should not evict the
+// moving volume from L2).
+constexpr int kPreZ = 8;
+
 template <typename TM>
 __global__ void __launch_bounds__(256) k_presample(const TM* __restrict__ mov, int mx, int my,
-                                                   int mz, int vx, int vy,
+                                                   int mz, int vx, int vy, int vz,
                                                    const Xform* __restrict__ xf, int k0,
                                                    float* __restrict__ out) {
-  __shared__ TileBase T;
-  __shared__ int s_in;
+  __shared__ int s_ib[kPreZ][3];
+  __shared__ float s_fb[kPreZ][3];
+  __shared__ float s_A[9];
+  __shared__ int s_in[kPreZ];
   const int ntx = (vx + 31) >> 5;
   const int x0 = (blockIdx.x % ntx) * 32, y0 = (blockIdx.x / ntx) * 8;
-  const int z = blockIdx.y, slot = blockIdx.z;
+  const int z0 = blockIdx.y * kPreZ, slot = blockIdx.z;
   const int tid = threadIdx.x;
   const Xform* X = xf + k0 + slot;
-  if (tid < 3) xform_coord(*X, tid, x0, y0, z, T.ib[tid], T.fb[tid]);
-  if (tid < 9) T.A[tid] = X->ah[tid];
+  if (tid < 3 * kPreZ) {
+    const int zs = tid / 3, a = tid - 3 * zs;
+    xform_coord(*X, a, x0, y0, z0 + zs, s_ib[zs][a], s_fb[zs][a]);
+  } else if (tid < 3 * kPreZ + 9) {
+    s_A[tid - 3 * kPreZ] = X->ah[tid - 3 * kPreZ];
+  }
   __syncthreads();
-  if (tid == 0) s_in = tile_inside(T, mx, my, mz) ? 1 : 0;
+  if (tid < kPreZ) {
+    TileBase T;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      T.ib[a] = s_ib[tid][a];
+      T.fb[a] = s_fb[tid][a];
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) T.A[i] = s_A[i];
+    s_in[tid] = tile_inside(T, mx, my, mz) ? 1 : 0;
+  }
   __syncthreads();
   const int tx = tid & 31, ty = tid >> 5;
   const int x = x0 + tx, y = y0 + ty;
   if (x >= vx || y >= vy) return;
-  const float v = s_in ? tile_sample_inside<TM>(mov, mx, my, T, tx, ty)
-                       : tile_sample<3, TM>(mov, mx, my, mz, T, tx, ty);
-  const size_t nv = (size_t)vx * vy * gridDim.y;
-  out[(size_t)slot * nv + ((size_t)z * vy + y) * vx + x] = v;
+  const size_t plane = (size_t)vx * vy;
+  float* dst = out + (size_t)slot * plane * vz + (size_t)y * vx + x;
+  float v[kPreZ];
+#pragma unroll
+  for (int zs = 0; zs < kPreZ; ++zs) {
+    TileBase T;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      T.ib[a] = s_ib[zs][a];
+      T.fb[a] = s_fb[zs][a];
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) T.A[i] = s_A[i];
+    v[zs] = s_in[zs] ? tile_sample_inside<TM>(mov, mx, my, T, tx, ty)
+                     : tile_sample<3, TM>(mov, mx, my, mz, T, tx, ty);
+  }
+#pragma unroll
+  for (int zs = 0; zs < kPreZ; ++zs)
+    if (z0 + zs < vz) __stcs(dst + (size_t)(z0 + zs) * plane, v[zs]);
 }
 
 // PRE: the moving image is read from a presampled buffer (k_presample, one
@@ -748,7 +785,7 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(ND, TY, R))
       if constexpr (PRE) {
         const float* src = pre_slot + (size_t)(zin ? zs : 0) * ((size_t)P.vx * P.vy);
 #pragma unroll
-        for (int k = 0; k < WP; ++k) out[k] = (zin && poff[k] >= 0) ? __ldg(src + poff[k]) : 0.0f;
+        for (int k = 0; k < WP; ++k) out[k] = (zin && poff[k] >= 0) ? __ldcs(src + poff[k]) : 0.0f;
         return;
       }
       if (s_inside) {
@@ -968,9 +1005,9 @@ template <typename T>
 cudaError_t presample_launch(const void* mov, const FusedParams& P, const Xform* xf, int k0,
                              int cnt, float* pre, cudaStream_t stream) {
   const int ntx = (P.vx + 31) / 32, nty = (P.vy + 7) / 8;
-  dim3 grid(ntx * nty, P.vz, cnt);
-  k_presample<T><<<grid, 256, 0, stream>>>((const T*)mov, P.mx, P.my, P.mz, P.vx, P.vy, xf, k0,
-                                           pre);
+  dim3 grid(ntx * nty, (P.vz + kPreZ - 1) / kPreZ, cnt);
+  k_presample<T><<<grid, 256, 0, stream>>>((const T*)mov, P.mx, P.my, P.mz, P.vx, P.vy, P.vz, xf,
+                                           k0, pre);
   return cudaGetLastError();
 }
 

@@ -76,7 +76,8 @@ def test_rigid_registration_matches_oracle(config):
     gpu, orc = _both(case, "f32", init, lo, hi, ["translation", "rotation"], maxeval)
     d = np.abs(gpu["params"] - orc["params"])
     assert d[:nr].max() <= (0.02 if case.mode == "2D" else 0.01), d   # mm and degrees
-    assert abs(gpu["lc2"] / orc["lc2"] - 1.0) < 1e-5
+    # values at the two optima (in 2D two points a hundredth of a pixel apart)
+    assert abs(gpu["lc2"] / orc["lc2"] - 1.0) < (1e-3 if case.mode == "2D" else 1e-5)
     assert np.abs(gpu["params"][:nr] - _truth(case)[:nr]).max() < 0.5
 
 
