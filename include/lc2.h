@@ -156,8 +156,8 @@ long long lc2_launch_count(const lc2_context* ctx);
 /* Tuning options (lc2_set_option). LC2_OPTION_TILE_ROWS: output rows per
  * tile of the fused 3D kernel: 16 (one CTA per SM), 24 (one 768-thread CTA
  * per SM; resampled MR/CT only, the resampled-ultrasound kernel takes it as
- * 16) or 8 (two per SM); 0 = automatic (24 for patch radius 3 or 4 where it
- * exists, else 16). 2D and 2D-to-3D contexts with a resampled MR/CT: 16 or
+ * 16) or 8 (two per SM); 0 = automatic (16; 24 for patch radius 3 or 4 when
+ * the kernel resamples itself, LC2_OPTION_PRESAMPLE 0). 2D and 2D-to-3D contexts with a resampled MR/CT: 16 or
  * 32 (two 1024-thread CTAs per SM, patch radius 4 to 6; other radii take
  * it as 16); 0 = per launch (32 where it exists and the launch has four
  * CTAs per SM or more). No counterpart in the
@@ -167,7 +167,7 @@ enum { LC2_OPTION_TILE_ROWS = 1 };
 /* LC2_OPTION_ZCHUNK: output slices each CTA of the fused 3D kernel marches
  * through (0 = automatic). LC2_OPTION_GRAPHS: 1 (default) replays
  * lc2_evaluate_batch / lc2_evaluate from a CUDA graph captured once per batch
- * size; 0 issues the calls one by one. None of the options changes a
+ * size; 0 issues the calls one by one. None of these options changes a
  * result: every sum is exact, whatever the tiling. */
 enum { LC2_OPTION_ZCHUNK = 2, LC2_OPTION_GRAPHS = 3 };
 /* LC2_OPTION_PIPELINE: 1 runs 3D evaluations with patch radius <= 4 on the
@@ -196,14 +196,17 @@ enum { LC2_OPTION_STREAM_PRIORITY = 5 };
  * The values agree to FP32 resampling rounding (the two paths place their
  * sampling bases differently). */
 enum { LC2_OPTION_GENERIC = 7 };
-/* LC2_OPTION_PRESAMPLE (3D, HighResolutionModality Moving): 1 runs the
- * resampling of the moving image as a pass of its own -- one float per
- * virtual voxel and transform, written to a context buffer of at most 4 GiB
- * (64 transforms at 256^3; larger batches go in groups) -- and the fused
- * kernel reads it instead of gathering; 0 resamples inside the fused kernel.
- * Each voxel is sampled once from its 32 x 8 tile's base in the first form,
- * from its fused tile's base in the second, so the two agree to FP32
- * resampling rounding, not bit for bit. */
+/* LC2_OPTION_PRESAMPLE (3D, HighResolutionModality Moving): how the moving
+ * image is resampled. 1 (the default of such contexts): in a pass of its own,
+ * one float per virtual voxel and transform written to a context buffer that
+ * grows with the batch up to 2 GiB (32 transforms at 256^3; larger batches
+ * run in groups), which the fused kernel then reads; 2: its Sobel magnitude
+ * in a second pass as well, and the moments kernel reads both; 0: inside the
+ * fused kernel. Each voxel is sampled once from its 32 x 8 tile's base in
+ * forms 1 and 2 (which give the same bits) and from the fused tile's base
+ * in form 0, so 0 and 1 agree to FP32 resampling rounding (about 1e-7
+ * relative on LC2), not bit for bit. Within a form no option changes a
+ * value. */
 enum { LC2_OPTION_PRESAMPLE = 8 };
 int lc2_set_option(lc2_context* ctx, int option, int value);
 

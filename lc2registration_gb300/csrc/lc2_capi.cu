@@ -18,6 +18,7 @@
 #include "lc2_kernels.cuh"
 #include "lc2_fused.cuh"
 #include "lc2_fused_fixed.cuh"
+#include "lc2_fused_pg.cuh"
 #include "lc2_list.cuh"
 #include "lc2_mi.cuh"
 
@@ -219,8 +220,8 @@ struct lc2_context {
   int zchunk = 0;     // fused kernel output slices per CTA (0 = automatic)
   int pipeline = 0;   // warp-specialised fused 3D kernel (LC2_OPTION_PIPELINE)
   int presample = 0;  // 3D: resample as a pass of its own (LC2_OPTION_PRESAMPLE)
-  float* d_pre = nullptr;  // presampled moving image, pre_slots transforms
-  int pre_slots = 0;
+  float* d_pre = nullptr;  // presampled images of pre_slots transforms (pre_planes each)
+  int pre_slots = 0, pre_planes = 0;
   int* d_err = nullptr;   // device flag of the warp-specialised kernel's bounded waits
   int* h_err = nullptr;   // pinned copy
 
@@ -620,23 +621,36 @@ int tile_rows(const lc2_context* c) {
   if (c->tile_rows > 0) return c->tile_rows;
   if (c->lc2_nd == 2) return 0;  // chosen per launch: 32 rows for large launches, else 16
   const int r = c->cfg.patch_size;
-  return (c->lc2_nd == 3 && c->cfg.high_res_is_moving && (r == 3 || r == 4)) ? 24 : 16;
+  // 24-row tiles (768 threads) pay where the fused kernel gathers; on
+  // presampled images the 16-row tiles (123 registers, no spills) are faster
+  return (c->lc2_nd == 3 && c->cfg.high_res_is_moving && !c->presample && (r == 3 || r == 4))
+             ? 24 : 16;
 }
 
 // The fused kernel (static ultrasound): one launch for `cnt` transforms.
-// Transforms per presample group: the buffer holds at most 4 GiB (64
-// transforms of a 256^3 grid), at most 64 transforms.
-constexpr size_t kPresampleBytes = size_t(4) << 30;
-int presample_slots(const lc2_context* c) {
-  const size_t per = sizeof(float) * c->nv;
+// The presample buffer holds the images of a group of transforms: M (and G
+// in the three-pass form) of up to presample_cap transforms, at most 2 GiB
+// and 64 transforms -- 32 at 256^3. It grows with the batches a context is
+// given (a registration's single evaluations hold one slot); growing moves
+// it, which drops the captured graphs that name it.
+constexpr size_t kPresampleBytes = size_t(2) << 30;
+int presample_planes(const lc2_context* c) { return c->presample == 2 ? 2 : 1; }
+int presample_cap(const lc2_context* c) {
+  const size_t per = sizeof(float) * c->nv * (size_t)presample_planes(c);
   return (int)std::max<size_t>(1, std::min<size_t>(64, kPresampleBytes / per));
 }
 
-int ensure_presample(lc2_context* c) {
-  if (c->d_pre) return LC2_OK;
-  const int slots = presample_slots(c);
-  LC2_CUDA(dev_alloc((void**)&c->d_pre, sizeof(float) * c->nv * (size_t)slots, c->stream));
-  c->pre_slots = slots;
+int ensure_presample(lc2_context* c, int count) {
+  const int want = std::max(1, std::min(count, presample_cap(c)));
+  if (c->d_pre && c->pre_slots >= want && c->pre_planes == presample_planes(c)) return LC2_OK;
+  drop_graphs(c);
+  dev_free(c->d_pre, c->stream);
+  c->d_pre = nullptr;
+  c->pre_slots = 0;
+  const int planes = presample_planes(c);
+  LC2_CUDA(dev_alloc((void**)&c->d_pre, sizeof(float) * c->nv * (size_t)planes * want, c->stream));
+  c->pre_slots = want;
+  c->pre_planes = planes;
   return LC2_OK;
 }
 
@@ -678,7 +692,7 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
   if (c->presample && c->lc2_nd == 3 && !c->pipeline) {
     // resample pass, then the fused kernel on the presampled images, in
     // groups of the presample buffer's capacity
-    LC2_TRY(ensure_presample(c));
+    LC2_TRY(ensure_presample(c, cnt));
     for (int j = 0; j < cnt; j += c->pre_slots) {
       const int n = std::min(c->pre_slots, cnt - j);
       {
@@ -695,8 +709,26 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
       LC2_CUDA(e);
       L.k0 = k0 + j;
       L.cnt = n;
-      L.pre = c->d_pre;
-      {
+      if (c->presample == 2 && c->cfg.patch_size <= 4) {
+        // three passes: the Sobel magnitude too, then the moments
+        float* dG = c->d_pre + (size_t)c->pre_slots * c->nv;
+        {
+          TimerScope ts(c, K_SOBEL);
+          e = lc2::presobel_launch(c->d_pre, c->fp, n, dG, c->stream);
+        }
+        ++c->launches;
+        LC2_CUDA(e);
+        {
+          TimerScope ts(c, K_MOMENTS);
+          if (c->cfg.storage == LC2_STORE_F16)
+            e = lc2::fused_pg_entry<__half>(L, c->d_pre, dG);
+          else if (c->cfg.storage == LC2_STORE_BF16)
+            e = lc2::fused_pg_entry<__nv_bfloat16>(L, c->d_pre, dG);
+          else
+            e = lc2::fused_pg_entry<float>(L, c->d_pre, dG);
+        }
+      } else {
+        L.pre = c->d_pre;
         TimerScope ts(c, K_MOMENTS);
         e = fused();
       }
@@ -927,6 +959,8 @@ int plan_context(const lc2_config* cfg, lc2_context* c) {
   slots = std::min<long long>(slots, 1024);
   slots = std::min<long long>(slots, 65535 / c->virt.dim[2]);
   c->slots = (int)std::max<long long>(1, slots);
+  // 3D contexts of a resampled MR/CT resample in a pass of their own
+  c->presample = (c->lc2_nd == 3 && cfg->high_res_is_moving && !c->mi) ? 1 : 0;
   return LC2_OK;
 }
 
@@ -944,6 +978,8 @@ void context_bytes(const lc2_context* c, size_t* held, size_t* peak_extra) {
   if (c->mi)
     h += c->nv + 64 * (sizeof(unsigned) * (lc2::kMiHist + 2) + sizeof(double) * 2 * lc2::kMiParts);
   h += 64 * (sizeof(lc2::Xform) + 2 * sizeof(unsigned long long) + sizeof(double));
+  if (c->presample)  // the presample buffer at its largest
+    h += sizeof(float) * c->nv * (size_t)presample_planes(c) * (size_t)presample_cap(c);
   *held = h;
   *peak_extra = std::max(c->nm, c->nf) * sizeof(float);
   if (!hrm && !c->mi)  // temporaries of the static sums
@@ -1154,8 +1190,8 @@ int lc2_set_option(lc2_context* c, int option, int value) {
     return LC2_OK;
   }
   if (option == LC2_OPTION_PRESAMPLE) {
-    if (value != 0 && value != 1) return fail(LC2_ERR_INVALID_ARGUMENT, "presample must be 0 or 1");
-    if (value == 1 && (c->lc2_nd != 3 || !c->cfg.high_res_is_moving || c->mi))
+    if (value < 0 || value > 2) return fail(LC2_ERR_INVALID_ARGUMENT, "presample must be 0, 1 or 2");
+    if (value != 0 && (c->lc2_nd != 3 || !c->cfg.high_res_is_moving || c->mi))
       return fail(LC2_ERR_UNSUPPORTED, "presampling exists for 3D LC2 contexts with "
                   "HighResolutionModality: Moving");
     c->presample = value;
@@ -1568,6 +1604,7 @@ namespace {
 int stage_host(lc2_context* c, const float* matrices, int count) {
   if (count < 0 || (count > 0 && !matrices)) return fail(LC2_ERR_INVALID_ARGUMENT, "bad transforms");
   LC2_TRY(ensure_capacity(c, count));
+  if (c->presample && !c->generic && !c->pipeline) LC2_TRY(ensure_presample(c, count));
   const int mf = matrix_floats(c);
   for (int k = 0; k < count; ++k) {
     const float* m = matrices + (size_t)k * mf;

@@ -1,0 +1,299 @@
+// lc2_fused_pg.cuh -- the fused 3D evaluation on presampled images.
+//
+// Three passes per group of transforms (LC2_OPTION_PRESAMPLE = 2):
+//   1. k_presample (lc2_fused.cuh): the moving image resampled onto the
+//      virtual grid, one float per voxel and transform
+//      (src/Interpolator/interpolator.cu:69-179);
+//   2. k_presobel: its Sobel gradient magnitude with zero padding
+//      (src/cu_LC2/cu_lc2_3d.cu:100-179), one float per voxel and transform;
+//   3. k_fused_pg: the z-marching moments, window sums and solve of k_fused,
+//      reading M and G of each entering slice straight from those buffers.
+// Without the resampled slice planes the fused pass needs no plane phase:
+// the limb planes are double-buffered, so a slice costs three barriers
+// (after the limb writes, after the x pass, after the y pass) and the solve
+// of slice z overlaps the limb writes of slice z+1. Every sum is exact, as in
+// k_fused; each voxel's M and G are computed once, so the value does not
+// depend on tiles, z chunks or groups.
+#pragma once
+
+#include "lc2_fused.cuh"
+
+namespace lc2 {
+
+// ---- pass 2: Sobel magnitude of presampled images ----
+// A CTA covers a 32 x 8 tile over kSobZ slices: the (34 x 10 x kSobZ+2)
+// region is loaded once (zero outside the grid), then per slice the
+// z-smoothed / z-differentiated plane (Sz, Dz) and the in-plane taps, with
+// the arithmetic of fused_sobel_sd.
+constexpr int kSobZ = 8;
+
+template <int ZS = kSobZ>
+__global__ void __launch_bounds__(256) k_presobel(const float* __restrict__ M, int vx, int vy,
+                                                  int vz, float* __restrict__ G) {
+  __shared__ float t[ZS + 2][10][34];
+  __shared__ float2 sd[10 * 34];
+  const int ntx = (vx + 31) >> 5;
+  const int x0 = (blockIdx.x % ntx) * 32, y0 = (blockIdx.x / ntx) * 8;
+  const int z0 = blockIdx.y * ZS, slot = blockIdx.z;
+  const int tid = threadIdx.x;
+  const size_t plane = (size_t)vx * vy, nv = plane * vz;
+  const float* src = M + (size_t)slot * nv;
+  for (int i = tid; i < (ZS + 2) * 10 * 34; i += 256) {
+    const int hz = i / 340, rem = i - hz * 340, hy = rem / 34, hx = rem - hy * 34;
+    const int gx = x0 + hx - 1, gy = y0 + hy - 1, gz = z0 + hz - 1;
+    float v = 0.0f;
+    if (gx >= 0 && gx < vx && gy >= 0 && gy < vy && gz >= 0 && gz < vz)
+      v = __ldcs(src + (size_t)gz * plane + (size_t)gy * vx + gx);
+    t[hz][hy][hx] = v;
+  }
+  __syncthreads();
+  const int tx = tid & 31, ty = tid >> 5;
+  const int x = x0 + tx, y = y0 + ty;
+  float* dst = G + (size_t)slot * nv + (size_t)y * vx + x;
+  for (int zs = 0; zs < ZS; ++zs) {
+    for (int i = tid; i < 340; i += 256) {
+      const int hy = i / 34, hx = i - hy * 34;
+      const float a = t[zs][hy][hx], b = t[zs + 1][hy][hx], c = t[zs + 2][hy][hx];
+      sd[i] = make_float2(a + 2.0f * b + c, c - a);
+    }
+    __syncthreads();
+    if (x < vx && y < vy && z0 + zs < vz)
+      __stcs(dst + (size_t)(z0 + zs) * plane, fused_sobel_sd<34>(sd, (ty + 1) * 34 + tx + 1));
+    __syncthreads();
+  }
+}
+
+// ---- pass 3: moments, window sums and solve ----
+constexpr int kPgTY = 16;
+
+template <int R>
+struct PgGeom {
+  static constexpr int TY = kPgTY;
+  static constexpr int NT = 32 * TY;
+  static constexpr int HX = 32 + 2 * R, HY = TY + 2 * R;
+  static constexpr int HXP = FusedGeom<3, TY, R>::HXP;
+  static constexpr int NP = HX * HY;
+  static constexpr int MAXP = (NP + NT - 1) / NT;
+  static constexpr int RING = 2 * R + 1;  // leaving qM, qG, qU of the z window
+  static constexpr size_t PA = (size_t)HY * HXP;  // ints per limb plane
+  static constexpr size_t OFF_A = sizeof(int) * (size_t)RING * 3 * NP;
+  static constexpr size_t BYTES = OFF_A + 2 * sizeof(int) * kLimbs * PA;  // two limb buffers
+  static_assert(R > 4 || BYTES + 1024 <= 227 * 1024, "one CTA's shared memory must fit an SM");
+};
+
+template <typename TS, int R>
+__global__ void __launch_bounds__(32 * kPgTY, 1)
+    k_fused_pg(const float* __restrict__ Mb, const float* __restrict__ Gb,
+               const TS* __restrict__ Ust, const float* __restrict__ sig,
+               const int* __restrict__ su, FusedParams P, int k0,
+               unsigned long long* __restrict__ acc, float* __restrict__ out_measure) {
+  using G = PgGeom<R>;
+  constexpr int NT = G::NT, TY = G::TY, MAXP = G::MAXP;
+  constexpr int KB = PatchConst<3, R>::K;
+  constexpr unsigned long long kmask = (1ull << KB) - 1ull;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int* lv = reinterpret_cast<int*>(smem_raw);
+  int* A0 = reinterpret_cast<int*>(smem_raw + G::OFF_A);
+  const int tid = threadIdx.x, slot = blockIdx.x, tile = blockIdx.y;
+  const int x0 = (tile % P.ntx) * 32, y0 = (tile / P.ntx) * TY;
+  const int ox = tid & 31, oy = tid >> 5;
+  const int zb = blockIdx.z * P.zchunk;
+  const int ze = min(zb + P.zchunk, P.vz);
+  const size_t slice = (size_t)P.vx * P.vy;
+  const float* Ms = Mb + (size_t)slot * slice * P.vz;
+  const float* Gs = Gb + (size_t)slot * slice * P.vz;
+  // the thread's halo points: in-slice offset (-1 outside the grid) and A offset
+  int pu[MAXP], pa_off[MAXP];
+#pragma unroll
+  for (int j = 0; j < MAXP; ++j) {
+    const int p = tid + j * NT;
+    const int hy = p / G::HX, hx = p - hy * G::HX;
+    const int gx = x0 - R + hx, gy = y0 - R + hy;
+    pa_off[j] = hy * G::HXP + hx;
+    pu[j] = (p < G::NP && gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy) ? gy * P.vx + gx : -1;
+  }
+  // exact z-window sums per halo point: qM, qG in int32, the products in int64
+  int accq[MAXP][2];
+  long long accp[MAXP][5];
+#pragma unroll
+  for (int j = 0; j < MAXP; ++j) {
+    accq[j][0] = accq[j][1] = 0;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) accp[j][k] = 0;
+  }
+  const int e0 = zb - R;  // first slice entering the window
+  // M, G and the static ultrasound of the entering slice, loaded an
+  // iteration ahead
+  float m_nx[MAXP], g_nx[MAXP], u_nx[MAXP];
+  auto load_in = [&](int e) {
+    const bool zin = (e >= 0 && e < P.vz);
+#pragma unroll
+    for (int j = 0; j < MAXP; ++j) {
+      const bool ok = zin && pu[j] >= 0;
+      const size_t o = (size_t)(zin ? e : 0) * slice + (pu[j] >= 0 ? pu[j] : 0);
+      m_nx[j] = ok ? __ldcs(Ms + o) : 0.0f;
+      g_nx[j] = ok ? __ldcs(Gs + o) : 0.0f;
+      u_nx[j] = ok ? ldf(Ust, o) : 0.0f;
+    }
+  };
+  // weighting factor and S_U of the thread's output voxel, a slice ahead
+  float sg_nx = 0.0f;
+  int sv_nx = 0;
+  auto load_sig = [&](int z) {
+    const int x = x0 + ox, y = y0 + oy;
+    sg_nx = 0.0f;
+    sv_nx = 0;
+    if (z >= zb && z < ze && x < P.vx && y < P.vy) {
+      const size_t gi = (size_t)z * slice + (size_t)y * P.vx + x;
+      sg_nx = __ldg(sig + gi);
+      sv_nx = __ldg(su + gi);
+    }
+  };
+  load_in(e0);
+  load_sig(e0 - R);
+  long long acc_m = 0;
+  int buf = 0;
+  for (int e = e0; e < ze + R; ++e) {
+    float m_in[MAXP], g_in[MAXP], u_in[MAXP];
+#pragma unroll
+    for (int j = 0; j < MAXP; ++j) {
+      m_in[j] = m_nx[j];
+      g_in[j] = g_nx[j];
+      u_in[j] = u_nx[j];
+    }
+    load_in(e + 1);
+    const int z = e - R;          // output slice completed by this entering slice
+    const float sg = sg_nx;
+    const int sv = sv_nx;
+    load_sig(z + 1);
+    const int l = e - 2 * R - 1;  // slice leaving the window
+    const bool out = (z >= zb);
+    const bool leave = (l >= e0);
+    int* A = A0 + (size_t)buf * kLimbs * G::PA;
+    int* lv_in = lv + ((e - e0) % G::RING) * 3 * G::NP;
+    const int* lv_out = lv + ((l - e0 + G::RING) % G::RING) * 3 * G::NP;
+#pragma unroll
+    for (int j = 0; j < MAXP; ++j) {
+      const int p = tid + j * NT;
+      if (p < G::NP) {
+        const int qm = quant(m_in[j], P.qm), qg = quant(g_in[j], P.qg), qu = quant(u_in[j], P.qu);
+        // the leaving slice's ring entry is the entering slice's: read it
+        // before it is overwritten (only this thread touches entry p)
+        if (leave) {
+          const int qml = lv_out[p], qgl = lv_out[G::NP + p], qul = lv_out[2 * G::NP + p];
+          accp[j][0] -= (long long)qul * qml;
+          accp[j][1] -= (long long)qul * qgl;
+          accp[j][2] -= (long long)qml * qml;
+          accp[j][3] -= (long long)qgl * qgl;
+          accp[j][4] -= (long long)qml * qgl;
+          accq[j][0] -= qml;
+          accq[j][1] -= qgl;
+        }
+        lv_in[p] = qm;
+        lv_in[G::NP + p] = qg;
+        lv_in[2 * G::NP + p] = qu;
+        accp[j][0] += (long long)qu * qm;
+        accp[j][1] += (long long)qu * qg;
+        accp[j][2] += (long long)qm * qm;
+        accp[j][3] += (long long)qg * qg;
+        accp[j][4] += (long long)qm * qg;
+        accq[j][0] += qm;
+        accq[j][1] += qg;
+        if (out) {
+          // limb layout of fused_limbs: qM, qG, then (lo, hi) per product
+          int* a = A + pa_off[j];
+          a[0] = accq[j][0];
+          a[G::PA] = accq[j][1];
+#pragma unroll
+          for (int k = 0; k < 5; ++k) {
+            a[(2 + 2 * k) * G::PA] = (int)((unsigned long long)accp[j][k] & kmask);
+            a[(3 + 2 * k) * G::PA] = (int)(accp[j][k] >> KB);
+          }
+        }
+      }
+    }
+    if (out) {
+      __syncthreads();
+      fused_xy<3, TY, R>(A);  // x pass, barrier, y pass, barrier
+      const int x = x0 + ox, y = y0 + oy;
+      if (x < P.vx && y < P.vy) {
+        float m = 0.0f;
+        if (sg > 0.0f) {
+          const int* a = A + oy * G::HXP + ox;
+          int L[kLimbs];
+#pragma unroll
+          for (int k = 0; k < kLimbs; ++k) L[k] = a[k * G::PA];
+          m = fused_measure<3, R>(P, sg, sv, L);
+          acc_m += __float2int_rn(m * P.sum_scale);
+        }
+        if (out_measure && slot == 0) out_measure[(size_t)z * slice + (size_t)y * P.vx + x] = m;
+      }
+      buf ^= 1;  // the next slice writes the other limb buffer while this one is solved
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc_m += __shfl_down_sync(0xffffffffu, acc_m, o);
+  if ((tid & 31) == 0) atomicAdd(acc + 2 * (size_t)(k0 + slot), (unsigned long long)acc_m);
+}
+
+template <typename T, int R>
+cudaError_t fused_pg_launch_r(const FusedLaunch& L, const float* M, const float* Gr) {
+  using G = PgGeom<R>;
+  if (L.P.kbits != PatchConst<3, R>::K || L.P.n != PatchConst<3, R>::N)
+    return cudaErrorInvalidValue;
+  auto kern = k_fused_pg<T, R>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)G::BYTES);
+  if (e != cudaSuccess) return e;
+  FusedParams P = L.P;
+  const int ntx = (P.vx + 31) / 32, nty = (P.vy + G::TY - 1) / G::TY;
+  P.ntx = ntx;
+  if (L.zchunk > 0)
+    P.zchunk = L.zchunk < P.vz ? L.zchunk : P.vz;
+  else
+    P.zchunk = auto_zchunk(P.vz, R, (long long)ntx * nty * L.cnt, (long long)L.sms);
+  const int nz = (P.vz + P.zchunk - 1) / P.zchunk;
+  dim3 grid(L.cnt, ntx * nty, nz);
+  kern<<<grid, G::NT, G::BYTES, L.stream>>>(M, Gr, (const T*)L.ust, L.sig, L.su, P, L.k0, L.acc,
+                                            L.out_measure);
+  return cudaGetLastError();
+}
+
+// Patch radius 1..4 (shared memory holds two limb buffers up to radius 4).
+template <typename T>
+cudaError_t fused_pg_launch(const FusedLaunch& L, const float* M, const float* Gr) {
+  switch (L.P.r) {
+    case 1: return fused_pg_launch_r<T, 1>(L, M, Gr);
+    case 2: return fused_pg_launch_r<T, 2>(L, M, Gr);
+    case 3: return fused_pg_launch_r<T, 3>(L, M, Gr);
+    case 4: return fused_pg_launch_r<T, 4>(L, M, Gr);
+  }
+  return cudaErrorInvalidValue;
+}
+
+// Defined per storage type in lc2_pg_{f32,f16,bf16}.cu.
+template <typename T>
+cudaError_t fused_pg_entry(const FusedLaunch& L, const float* M, const float* Gr);
+template <>
+cudaError_t fused_pg_entry<float>(const FusedLaunch& L, const float* M, const float* Gr);
+template <>
+cudaError_t fused_pg_entry<__half>(const FusedLaunch& L, const float* M, const float* Gr);
+template <>
+cudaError_t fused_pg_entry<__nv_bfloat16>(const FusedLaunch& L, const float* M, const float* Gr);
+
+#define LC2_DEFINE_FUSED_PG(T)                                                              \
+  template <>                                                                               \
+  cudaError_t fused_pg_entry<T>(const FusedLaunch& L, const float* M, const float* Gr) {    \
+    return fused_pg_launch<T>(L, M, Gr);                                                    \
+  }
+
+// k_presobel of `cnt` presampled images.
+inline cudaError_t presobel_launch(const float* M, const FusedParams& P, int cnt, float* Gr,
+                                   cudaStream_t stream) {
+  const int ntx = (P.vx + 31) / 32, nty = (P.vy + 7) / 8;
+  dim3 grid(ntx * nty, (P.vz + kSobZ - 1) / kSobZ, cnt);
+  k_presobel<kSobZ><<<grid, 256, 0, stream>>>(M, P.vx, P.vy, P.vz, Gr);
+  return cudaGetLastError();
+}
+
+}  // namespace lc2
