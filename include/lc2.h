@@ -214,10 +214,11 @@ int lc2_set_option(lc2_context* ctx, int option, int value);
 long long lc2_graph_launches(const lc2_context* ctx);
 
 /* Autotuner: times the fused kernel on `count` transforms (matrices as in
- * lc2_evaluate_batch) for each tile height, kernel variant (single-role or
- * warp-specialised, LC2_OPTION_PIPELINE) and z-chunk length it supports,
+ * lc2_evaluate_batch) for each tile height and z-chunk length it supports,
  * keeps the fastest as the context's options and returns the tile height
- * and z chunk. Contexts
+ * and z chunk. It never changes a value: the warp-specialised kernel
+ * (LC2_OPTION_PIPELINE) and the resampling form (LC2_OPTION_PRESAMPLE) stay
+ * as the caller set them. Contexts
  * without a tunable kernel (2D windows, mutual information, the generic
  * path) return their current settings. The reference takes fixed block sizes as
  * arguments (src/cu_LC2/cu_lc2_3d.cuh:36-41). */

@@ -730,7 +730,17 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
       } else {
         L.pre = c->d_pre;
         TimerScope ts(c, K_MOMENTS);
-        e = fused();
+        if (c->cfg.patch_size <= 4) {
+          // the moments pass with the in-kernel Sobel on double-buffered limb planes
+          if (c->cfg.storage == LC2_STORE_F16)
+            e = lc2::fused_pg_entry<__half>(L, c->d_pre, nullptr);
+          else if (c->cfg.storage == LC2_STORE_BF16)
+            e = lc2::fused_pg_entry<__nv_bfloat16>(L, c->d_pre, nullptr);
+          else
+            e = lc2::fused_pg_entry<float>(L, c->d_pre, nullptr);
+        } else {
+          e = fused();
+        }
       }
       ++c->launches;
       LC2_CUDA(e);
@@ -2526,8 +2536,9 @@ extern "C" int lc2_autotune(lc2_context* c, const float* matrices, int count, in
       int rows, pipeline;
     };
     std::vector<Cand> cands;
+    // the warp-specialised kernel never won a trial and resamples in place
+    // (other bits than the default presampled form): selectable, not a candidate
     for (int tr : rows) cands.push_back({tr, 0});
-    if (r <= 4 && hrm) cands.push_back({16, 1});
     for (const Cand& cd : cands) {
       const int tr = cd.rows;
       for (int zc : chunks) {

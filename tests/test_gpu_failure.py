@@ -19,6 +19,8 @@ def test_expired_wait_is_reported_and_context_stays_usable():
     case = synth.case_3d(seed=41, mr_size=40, us_size=32, r=2, blobs=5)
     ctx = make_context(case, "f16")
     mats = perturbed(case, np.random.default_rng(9), 5)
+    # the warp-specialised kernel resamples in place: compare with that form
+    ctx.set_option(capi.OPTION_PRESAMPLE, 0)
     before = ctx.evaluate_batch(mats)
     t0 = time.perf_counter()
     with pytest.raises(capi.LC2Error, match="LC2_ERR_TIMEOUT"):
