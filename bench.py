@@ -796,7 +796,10 @@ def main():
     if os.path.exists(tfile):
         try:
             tj = json.load(open(tfile))
-            traffic = tj.get("bytes_per_launch_scaled")
+            # DRAM bytes of the moments pass over the step's launches: it reads
+            # each transform's presampled image, so it scales with K
+            per_t = tj.get("dram_bytes_per_transform")
+            traffic = int(per_t * K) if per_t else tj.get("bytes_per_launch_scaled")
             ipv = tj.get("thread_instructions_per_voxel")
             captured = tj.get("captured_at")
         except Exception:
@@ -871,7 +874,10 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "traffic_source": from_profile,
-                         "kernel": "k_fused", "kernel_ms_per_launch": mom_ms / max(1, mom_launches),
+                         "kernel": "k_fused_ps (moments pass; the resample pass is kernels_ms_per_step.warp)",
+                         "launches_per_step": mom_launches,
+                         "kernel_ms_per_launch": mom_ms / max(1, mom_launches),
+                         "scope": "achieved and traffic are totals of the step's moments launches",
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
             "issue_roofline": issue_roofline(ipv, K * n_vox, mom_ms, local, clk, from_profile),
             "kernels_ms_per_step": {k: v[0] for k, v in kt.items()},
