@@ -634,7 +634,9 @@ int tile_rows(const lc2_context* c) {
 // given (a registration's single evaluations hold one slot); growing moves
 // it, which drops the captured graphs that name it.
 constexpr size_t kPresampleBytes = size_t(2) << 30;
-int presample_planes(const lc2_context* c) { return c->presample == 2 ? 2 : 1; }
+int presample_planes(const lc2_context* c) {
+  return (c->presample == 2 && c->cfg.high_res_is_moving) ? 2 : 1;
+}
 int presample_cap(const lc2_context* c) {
   const size_t per = sizeof(float) * c->nv * (size_t)presample_planes(c);
   return (int)std::max<size_t>(1, std::min<size_t>(64, kPresampleBytes / per));
@@ -781,13 +783,44 @@ int launch_fused_fixed(lc2_context* c, int k0, int cnt) {
   L.zchunk = c->zchunk;
   L.sms = c->sms;
   L.stream = c->stream;
-  TimerScope ts(c, K_MOMENTS);
+  auto fixed = [&]() {
+    TimerScope ts(c, K_MOMENTS);
+    switch (c->cfg.storage) {
+      case LC2_STORE_F16: return lc2::fixed_launch<__half>(L);
+      case LC2_STORE_BF16: return lc2::fixed_launch<__nv_bfloat16>(L);
+      default: return lc2::fixed_launch<float>(L);
+    }
+  };
   cudaError_t e;
-  switch (c->cfg.storage) {
-    case LC2_STORE_F16: e = lc2::fixed_launch<__half>(L); break;
-    case LC2_STORE_BF16: e = lc2::fixed_launch<__nv_bfloat16>(L); break;
-    default: e = lc2::fixed_launch<float>(L); break;
+  if (c->presample && c->lc2_nd == 3) {
+    // the ultrasound resampled in a pass of its own, then the moments, in
+    // groups of the presample buffer's capacity
+    LC2_TRY(ensure_presample(c, cnt));
+    for (int j = 0; j < cnt; j += c->pre_slots) {
+      const int n = std::min(c->pre_slots, cnt - j);
+      {
+        TimerScope ts(c, K_WARP);
+        if (c->cfg.storage == LC2_STORE_F16)
+          e = lc2::presample_launch<__half>(c->d_moving, c->fp, c->d_xf, k0 + j, n, c->d_pre, c->stream);
+        else if (c->cfg.storage == LC2_STORE_BF16)
+          e = lc2::presample_launch<__nv_bfloat16>(c->d_moving, c->fp, c->d_xf, k0 + j, n, c->d_pre,
+                                                   c->stream);
+        else
+          e = lc2::presample_launch<float>(c->d_moving, c->fp, c->d_xf, k0 + j, n, c->d_pre, c->stream);
+      }
+      ++c->launches;
+      LC2_CUDA(e);
+      L.k0 = k0 + j;
+      L.cnt = n;
+      L.pre = c->d_pre;
+      e = fixed();
+      ++c->launches;
+      if (e != cudaSuccess)
+        return fail(LC2_ERR_CUDA, "fused kernel (resampled ultrasound): %s", cudaGetErrorString(e));
+    }
+    return LC2_OK;
   }
+  e = fixed();
   ++c->launches;
   if (e != cudaSuccess) return fail(LC2_ERR_CUDA, "fused kernel (resampled ultrasound): %s", cudaGetErrorString(e));
   return LC2_OK;
@@ -970,7 +1003,7 @@ int plan_context(const lc2_config* cfg, lc2_context* c) {
   slots = std::min<long long>(slots, 65535 / c->virt.dim[2]);
   c->slots = (int)std::max<long long>(1, slots);
   // 3D contexts of a resampled MR/CT resample in a pass of their own
-  c->presample = (c->lc2_nd == 3 && cfg->high_res_is_moving && !c->mi) ? 1 : 0;
+  c->presample = (c->lc2_nd == 3 && !c->mi) ? 1 : 0;
   return LC2_OK;
 }
 
@@ -1201,9 +1234,8 @@ int lc2_set_option(lc2_context* c, int option, int value) {
   }
   if (option == LC2_OPTION_PRESAMPLE) {
     if (value < 0 || value > 2) return fail(LC2_ERR_INVALID_ARGUMENT, "presample must be 0, 1 or 2");
-    if (value != 0 && (c->lc2_nd != 3 || !c->cfg.high_res_is_moving || c->mi))
-      return fail(LC2_ERR_UNSUPPORTED, "presampling exists for 3D LC2 contexts with "
-                  "HighResolutionModality: Moving");
+    if (value != 0 && (c->lc2_nd != 3 || c->mi))
+      return fail(LC2_ERR_UNSUPPORTED, "presampling exists for 3D LC2 contexts");
     c->presample = value;
     drop_graphs(c);
     return LC2_OK;

@@ -101,10 +101,14 @@ __device__ __forceinline__ void fixed_flush(long long acc_m, long long acc_s,
 }
 
 // ---- 3D: z-marching over output slices [zb, ze) ----
-template <typename TM, int TY, int R>
+// PRE: the warped ultrasound is read from a presampled buffer (k_presample,
+// one float per virtual voxel and transform of the launch, slot-major)
+// instead of being resampled by the CTA.
+template <typename TM, int TY, int R, bool PRE = false>
 __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
     k_fused_fixed3(const TM* __restrict__ mov, FixedStatic S, FusedParams P,
-                   const Xform* __restrict__ xf, int k0, unsigned long long* __restrict__ acc) {
+                   const Xform* __restrict__ xf, int k0, unsigned long long* __restrict__ acc,
+                   const float* __restrict__ pre = nullptr) {
   using G = FusedGeom<3, TY, R>;
   using F = FixedGeom<3, TY, R>;
   constexpr int NT = G::NT, MAXP = G::MAXP, NL = kFixedLimbs;
@@ -134,6 +138,7 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
   const size_t slice = (size_t)P.vx * P.vy;
 
   auto set_base = [&](int zs) {
+    if (PRE) return;
     if (tid == NT - 1)
       s_inside = region_base<3, G::PW, G::PH>(s_xf, s_A, P, gx0, gy0, yb, zs,
                                               zs >= 0 && zs < P.vz, s_ib, s_fb)
@@ -208,13 +213,17 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
   //   3: y window pass into Y.
   bool pending = false;  // Y holds the patch sums of output slice z-1
   int nqm[MAXP], nqg[MAXP];  // static qM, qG of the next entering slice
+  float nu[PRE ? MAXP : 1];   // presampled ultrasound of the next entering slice
+  const float* pre_slot = PRE ? pre + (size_t)slot * slice * P.vz : nullptr;
 #pragma unroll
   for (int j = 0; j < MAXP; ++j) {
     nqm[j] = nqg[j] = 0;
+    if constexpr (PRE) nu[j] = 0.0f;
     if (pin[j] && e0 >= 0 && e0 < P.vz) {
       const size_t gi = (size_t)e0 * slice + pu[j];
       nqm[j] = __ldg(S.q + gi);
       nqg[j] = __ldg(S.q + S.nv + gi);
+      if constexpr (PRE) nu[j] = __ldcs(pre_slot + gi);
     }
   }
   for (int e = e0; e < ze + R; ++e) {
@@ -234,7 +243,9 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
       if (p < G::NP) {
         float u = 0.0f;
         int qm = 0, qg = 0;
-        if (inside) {
+        if constexpr (PRE) {
+          u = nu[j];
+        } else if (inside) {
           u = fused_sample_inside<TM>(mov, P, s_A, s_ib, s_fb, ppx[j], ppy[j]);
         } else if (pin[j] && zin) {
           u = fused_sample<3, TM>(mov, P, s_A, s_ib, s_fb, ppx[j], ppy[j]);
@@ -269,10 +280,12 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
 #pragma unroll
       for (int j = 0; j < MAXP; ++j) {
         nqm[j] = nqg[j] = 0;
+        if constexpr (PRE) nu[j] = 0.0f;
         if (pin[j] && zn) {
           const size_t gi = (size_t)(e + 1) * slice + pu[j];
           nqm[j] = __ldg(S.q + gi);
           nqg[j] = __ldg(S.q + S.nv + gi);
+          if constexpr (PRE) nu[j] = __ldcs(pre_slot + gi);
         }
       }
     }
@@ -362,14 +375,23 @@ struct FixedLaunch {
   int zchunk;       // 3D: output slices per CTA; 0 = automatic
   int sms;          // multiprocessors of the device
   cudaStream_t stream;
+  const float* pre = nullptr;  // 3D: presampled ultrasound of the launch (k_presample)
 };
+
+template <typename T, int R, int TY, typename K>
+cudaError_t fixed_launch3_k(const FixedLaunch& L, K kern);
 
 template <typename T, int R, int TY>
 cudaError_t fixed_launch3(const FixedLaunch& L) {
-  using F = FixedGeom<3, TY, R>;
   if (L.P.kbits != PatchConst<3, R>::K || L.P.n != PatchConst<3, R>::N)
     return cudaErrorInvalidValue;
-  auto kern = k_fused_fixed3<T, TY, R>;
+  if (L.pre) return fixed_launch3_k<T, R, TY>(L, k_fused_fixed3<T, TY, R, true>);
+  return fixed_launch3_k<T, R, TY>(L, k_fused_fixed3<T, TY, R, false>);
+}
+
+template <typename T, int R, int TY, typename K>
+cudaError_t fixed_launch3_k(const FixedLaunch& L, K kern) {
+  using F = FixedGeom<3, TY, R>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)F::BYTES);
   if (e != cudaSuccess) return e;
@@ -383,7 +405,8 @@ cudaError_t fixed_launch3(const FixedLaunch& L) {
                            (long long)L.sms * fused_min_blocks(3, TY, R));
   const int nz = (P.vz + P.zchunk - 1) / P.zchunk;
   dim3 grid(L.cnt, ntx * nty, nz);
-  kern<<<grid, 32 * TY, F::BYTES, L.stream>>>((const T*)L.mov, L.S, P, L.xf, L.k0, L.acc);
+  kern<<<grid, 32 * TY, F::BYTES, L.stream>>>((const T*)L.mov, L.S, P, L.xf, L.k0, L.acc,
+                                               L.pre);
   return cudaGetLastError();
 }
 

@@ -197,3 +197,35 @@ def test_presample_forms(r, storage):
     for k in (0, 10):
         want = oracle_eval(case, mats[k], storage=storage)
         assert abs(ref[k] / want - 1.0) < 1e-5, (k, ref[k], want)
+
+
+@pytest.mark.parametrize("r,storage", [(2, "f32"), (4, "f16")])
+def test_presample_fixed_modality(r, storage):
+    """HighResolutionModality: Fixed with the warped ultrasound presampled (the
+    default for 3D): the same bits whatever the tile height, z chunk or batch,
+    within FP32 resampling rounding of the in-kernel resampling, and within
+    1e-5 of the FP64 oracle."""
+    from tests.helpers import oracle_eval
+
+    base = synth.case_3d(seed=70 + r, mr_size=48, us_size=40, r=r, blobs=6)
+    inv = np.linalg.inv(base.true_mat.astype(np.float64)).astype(np.float32)
+    case = synth.Case(base.mode, base.moving_geom, base.moving, base.fixed_geom, base.fixed,
+                      [1.0, 1.0, 1.0], r, hr_moving=False, true_params={}, true_mat=inv)
+    ctx = make_context(case, storage)
+    mats = np.linalg.inv(perturbed(base, np.random.default_rng(r), 9).astype(np.float64))
+    mats = mats.astype(np.float32)
+    ref = ctx.evaluate_batch(mats)
+    np.testing.assert_array_equal([ctx.evaluate(m) for m in mats[:2]], ref[:2])
+    for rows in (16, 8):
+        ctx.set_option(capi.OPTION_TILE_ROWS, rows)
+        for zc in (0, 7):
+            ctx.set_option(capi.OPTION_ZCHUNK, zc)
+            np.testing.assert_array_equal(ctx.evaluate_batch(mats), ref)
+    ctx.set_option(capi.OPTION_TILE_ROWS, 0)
+    ctx.set_option(capi.OPTION_ZCHUNK, 0)
+    ctx.set_option(capi.OPTION_PRESAMPLE, 0)
+    inkernel = ctx.evaluate_batch(mats)
+    assert np.max(np.abs(inkernel / ref - 1.0)) < 2e-6
+    for k in (0, 8):
+        want = oracle_eval(case, mats[k], storage=storage)
+        assert abs(ref[k] / want - 1.0) < 1e-5, (k, ref[k], want)
