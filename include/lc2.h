@@ -200,12 +200,11 @@ enum { LC2_OPTION_GENERIC = 7 };
  * image is resampled. 1 (the default of such contexts): in a pass of its own,
  * one float per virtual voxel and transform written to a context buffer that
  * grows with the batch up to 2 GiB (32 transforms at 256^3; larger batches
- * run in groups), which the fused kernel then reads; 2: its Sobel magnitude
- * in a second pass as well, and the moments kernel reads both; 0: inside the
- * fused kernel. Each voxel is sampled once from its 32 x 8 tile's base in
- * forms 1 and 2 (which give the same bits) and from the fused tile's base
- * in form 0, so 0 and 1 agree to FP32 resampling rounding (about 1e-7
- * relative on LC2), not bit for bit. Within a form no option changes a
+ * run in groups), which the fused kernel then reads; 0: inside the fused
+ * kernel. Other values are refused (LC2_ERR_INVALID_ARGUMENT). Each voxel is
+ * sampled once from its 32 x 8 tile's base in form 1 and from the fused
+ * tile's base in form 0, so 0 and 1 agree to FP32 resampling rounding (about
+ * 1e-7 relative on LC2), not bit for bit. Within a form no option changes a
  * value. */
 enum { LC2_OPTION_PRESAMPLE = 8 };
 int lc2_set_option(lc2_context* ctx, int option, int value);

@@ -17,11 +17,11 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(OUT_DIR, "liblc2.so")
 SOURCES = ["lc2_capi.cu", "lc2_fused_f32.cu", "lc2_fused_f16.cu", "lc2_fused_bf16.cu",
            "lc2_list_f32.cu", "lc2_list_f16.cu", "lc2_list_bf16.cu", "lc2_fixed_f32.cu",
-           "lc2_fixed_f16.cu", "lc2_fixed_bf16.cu", "lc2_pg_f32.cu", "lc2_pg_f16.cu",
-           "lc2_pg_bf16.cu", "lc2_noalloc.cu",
+           "lc2_fixed_f16.cu", "lc2_fixed_bf16.cu", "lc2_ps_f32.cu", "lc2_ps_f16.cu",
+           "lc2_ps_bf16.cu", "lc2_noalloc.cu",
            "lc2_export.cu", "lc2_optim.cpp", "lc2_serve.cpp", "lc2_stack_reg.cpp"]
 DEPS = SOURCES + ["lc2_kernels.cuh", "lc2_fused.cuh", "lc2_fused_ws.cuh", "lc2_list.cuh",
-                   "lc2_mi.cuh", "lc2_fused_fixed.cuh", "lc2_fused_pg.cuh"]
+                   "lc2_mi.cuh", "lc2_fused_fixed.cuh", "lc2_fused_ps.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

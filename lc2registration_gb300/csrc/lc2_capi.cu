@@ -18,7 +18,7 @@
 #include "lc2_kernels.cuh"
 #include "lc2_fused.cuh"
 #include "lc2_fused_fixed.cuh"
-#include "lc2_fused_pg.cuh"
+#include "lc2_fused_ps.cuh"
 #include "lc2_list.cuh"
 #include "lc2_mi.cuh"
 
@@ -220,8 +220,8 @@ struct lc2_context {
   int zchunk = 0;     // fused kernel output slices per CTA (0 = automatic)
   int pipeline = 0;   // warp-specialised fused 3D kernel (LC2_OPTION_PIPELINE)
   int presample = 0;  // 3D: resample as a pass of its own (LC2_OPTION_PRESAMPLE)
-  float* d_pre = nullptr;  // presampled images of pre_slots transforms (pre_planes each)
-  int pre_slots = 0, pre_planes = 0;
+  float* d_pre = nullptr;  // presampled images (FP32 M) of pre_slots transforms
+  int pre_slots = 0;
   int* d_err = nullptr;   // device flag of the warp-specialised kernel's bounded waits
   int* h_err = nullptr;   // pinned copy
 
@@ -628,31 +628,25 @@ int tile_rows(const lc2_context* c) {
 }
 
 // The fused kernel (static ultrasound): one launch for `cnt` transforms.
-// The presample buffer holds the images of a group of transforms: M (and G
-// in the three-pass form) of up to presample_cap transforms, at most 2 GiB
-// and 64 transforms -- 32 at 256^3. It grows with the batches a context is
+// The presample buffer holds the images of a group of transforms, at most
+// 2 GiB and 64 transforms -- 32 at 256^3. It grows with the batches a context is
 // given (a registration's single evaluations hold one slot); growing moves
 // it, which drops the captured graphs that name it.
 constexpr size_t kPresampleBytes = size_t(2) << 30;
-int presample_planes(const lc2_context* c) {
-  return (c->presample == 2 && c->cfg.high_res_is_moving) ? 2 : 1;
-}
 int presample_cap(const lc2_context* c) {
-  const size_t per = sizeof(float) * c->nv * (size_t)presample_planes(c);
+  const size_t per = sizeof(float) * c->nv;
   return (int)std::max<size_t>(1, std::min<size_t>(64, kPresampleBytes / per));
 }
 
 int ensure_presample(lc2_context* c, int count) {
   const int want = std::max(1, std::min(count, presample_cap(c)));
-  if (c->d_pre && c->pre_slots >= want && c->pre_planes == presample_planes(c)) return LC2_OK;
+  if (c->d_pre && c->pre_slots >= want) return LC2_OK;
   drop_graphs(c);
   dev_free(c->d_pre, c->stream);
   c->d_pre = nullptr;
   c->pre_slots = 0;
-  const int planes = presample_planes(c);
-  LC2_CUDA(dev_alloc((void**)&c->d_pre, sizeof(float) * c->nv * (size_t)planes * want, c->stream));
+  LC2_CUDA(dev_alloc((void**)&c->d_pre, sizeof(float) * c->nv * (size_t)want, c->stream));
   c->pre_slots = want;
-  c->pre_planes = planes;
   return LC2_OK;
 }
 
@@ -711,35 +705,17 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
       LC2_CUDA(e);
       L.k0 = k0 + j;
       L.cnt = n;
-      if (c->presample == 2 && c->cfg.patch_size <= 4) {
-        // three passes: the Sobel magnitude too, then the moments
-        float* dG = c->d_pre + (size_t)c->pre_slots * c->nv;
-        {
-          TimerScope ts(c, K_SOBEL);
-          e = lc2::presobel_launch(c->d_pre, c->fp, n, dG, c->stream);
-        }
-        ++c->launches;
-        LC2_CUDA(e);
-        {
-          TimerScope ts(c, K_MOMENTS);
-          if (c->cfg.storage == LC2_STORE_F16)
-            e = lc2::fused_pg_entry<__half>(L, c->d_pre, dG);
-          else if (c->cfg.storage == LC2_STORE_BF16)
-            e = lc2::fused_pg_entry<__nv_bfloat16>(L, c->d_pre, dG);
-          else
-            e = lc2::fused_pg_entry<float>(L, c->d_pre, dG);
-        }
-      } else {
+      {
         L.pre = c->d_pre;
         TimerScope ts(c, K_MOMENTS);
         if (c->cfg.patch_size <= 4) {
           // the moments pass with the in-kernel Sobel on double-buffered limb planes
           if (c->cfg.storage == LC2_STORE_F16)
-            e = lc2::fused_pg_entry<__half>(L, c->d_pre, nullptr);
+            e = lc2::fused_ps_entry<__half>(L, c->d_pre);
           else if (c->cfg.storage == LC2_STORE_BF16)
-            e = lc2::fused_pg_entry<__nv_bfloat16>(L, c->d_pre, nullptr);
+            e = lc2::fused_ps_entry<__nv_bfloat16>(L, c->d_pre);
           else
-            e = lc2::fused_pg_entry<float>(L, c->d_pre, nullptr);
+            e = lc2::fused_ps_entry<float>(L, c->d_pre);
         } else {
           e = fused();
         }
@@ -1022,7 +998,7 @@ void context_bytes(const lc2_context* c, size_t* held, size_t* peak_extra) {
     h += c->nv + 64 * (sizeof(unsigned) * (lc2::kMiHist + 2) + sizeof(double) * 2 * lc2::kMiParts);
   h += 64 * (sizeof(lc2::Xform) + 2 * sizeof(unsigned long long) + sizeof(double));
   if (c->presample)  // the presample buffer at its largest
-    h += sizeof(float) * c->nv * (size_t)presample_planes(c) * (size_t)presample_cap(c);
+    h += sizeof(float) * c->nv * (size_t)presample_cap(c);
   *held = h;
   *peak_extra = std::max(c->nm, c->nf) * sizeof(float);
   if (!hrm && !c->mi)  // temporaries of the static sums
@@ -1233,7 +1209,7 @@ int lc2_set_option(lc2_context* c, int option, int value) {
     return LC2_OK;
   }
   if (option == LC2_OPTION_PRESAMPLE) {
-    if (value < 0 || value > 2) return fail(LC2_ERR_INVALID_ARGUMENT, "presample must be 0, 1 or 2");
+    if (value != 0 && value != 1) return fail(LC2_ERR_INVALID_ARGUMENT, "presample must be 0 or 1");
     if (value != 0 && (c->lc2_nd != 3 || c->mi))
       return fail(LC2_ERR_UNSUPPORTED, "presampling exists for 3D LC2 contexts");
     c->presample = value;

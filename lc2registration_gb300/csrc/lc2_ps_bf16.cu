@@ -1,0 +1,7 @@
+// The 3D moments pass on presampled images for bf16 storage of the static
+// ultrasound (patch radius 1-4), one translation unit per storage type.
+#include "lc2_fused_ps.cuh"
+
+namespace lc2 {
+LC2_DEFINE_FUSED_PS(__nv_bfloat16)
+}  // namespace lc2

@@ -170,10 +170,10 @@ def test_2d_tile_heights_agree_and_match_oracle(kind, storage):
 
 @pytest.mark.parametrize("r,storage", [(1, "f32"), (3, "f16"), (4, "bf16")])
 def test_presample_forms(r, storage):
-    """LC2_OPTION_PRESAMPLE: the resample pass (1, the default) and the
-    resample + Sobel passes (2) give the same bits, whatever the tile height,
-    z chunk, group size or batch; both agree with the in-kernel resampling
-    (0) to FP32 resampling rounding and with the FP64 oracle to 1e-5."""
+    """LC2_OPTION_PRESAMPLE: the resample pass (1, the default) gives the
+    same bits whatever the tile height, z chunk, group size or batch, agrees
+    with the in-kernel resampling (0) to FP32 resampling rounding and with the
+    FP64 oracle to 1e-5; other values are refused."""
     from tests.helpers import oracle_eval
 
     case = synth.case_3d(seed=60 + r, mr_size=48, us_size=40, r=r, blobs=6)
@@ -181,14 +181,15 @@ def test_presample_forms(r, storage):
     mats = perturbed(case, np.random.default_rng(r), 11)
     ref = ctx.evaluate_batch(mats)
     np.testing.assert_array_equal([ctx.evaluate(m) for m in mats[:3]], ref[:3])
-    for form in (2, 1):
-        ctx.set_option(capi.OPTION_PRESAMPLE, form)
-        for rows in (16, 24, 8) if r <= 4 else (8,):
-            ctx.set_option(capi.OPTION_TILE_ROWS, rows)
-            for zc in (0, 7):
-                ctx.set_option(capi.OPTION_ZCHUNK, zc)
-                np.testing.assert_array_equal(ctx.evaluate_batch(mats), ref)
-        np.testing.assert_array_equal(_staged(ctx, mats), ref)
+    with pytest.raises(capi.LC2Error, match="INVALID_ARGUMENT"):
+        ctx.set_option(capi.OPTION_PRESAMPLE, 2)
+    ctx.set_option(capi.OPTION_PRESAMPLE, 1)
+    for rows in (16, 24, 8) if r <= 4 else (8,):
+        ctx.set_option(capi.OPTION_TILE_ROWS, rows)
+        for zc in (0, 7):
+            ctx.set_option(capi.OPTION_ZCHUNK, zc)
+            np.testing.assert_array_equal(ctx.evaluate_batch(mats), ref)
+    np.testing.assert_array_equal(_staged(ctx, mats), ref)
     ctx.set_option(capi.OPTION_TILE_ROWS, 0)
     ctx.set_option(capi.OPTION_ZCHUNK, 0)
     ctx.set_option(capi.OPTION_PRESAMPLE, 0)
