@@ -73,7 +73,7 @@ def parse():
                     help="skip the registration (recovered-parameter) lines")
     ap.add_argument("--stack-frames", type=int, default=64)
     ap.add_argument("--stack-poses", type=int, default=256)
-    ap.add_argument("--serve-requests", type=int, default=100, help="requests per offered rate")
+    ap.add_argument("--serve-requests", type=int, default=200, help="requests per offered rate")
     ap.add_argument("--serve-rates", default="10,50,100,250,500",
                     help="offered Poisson arrival rates (requests/s), comma-separated")
     ap.add_argument("--serve-active", type=int, default=8)

@@ -156,8 +156,11 @@ long long lc2_launch_count(const lc2_context* ctx);
 /* Tuning options (lc2_set_option). LC2_OPTION_TILE_ROWS: output rows per
  * tile of the fused 3D kernel: 16 (one CTA per SM), 24 (one 768-thread CTA
  * per SM; resampled MR/CT only, the resampled-ultrasound kernel takes it as
- * 16) or 8 (two per SM); 0 = automatic (16; 24 for patch radius 3 or 4 when
- * the kernel resamples itself, LC2_OPTION_PRESAMPLE 0). 2D and 2D-to-3D contexts with a resampled MR/CT: 16 or
+ * 16) or 8 (two per SM); 0 = automatic (for a resampled MR/CT 24 at patch
+ * radius 1-4 on presampled images and at radius 3 or 4 when the kernel
+ * resamples itself, LC2_OPTION_PRESAMPLE 0; else 16). On presampled images
+ * at radius 1-4, 24 selects the 768-thread moments kernel and 8 or 16 the
+ * 512-thread one. 2D and 2D-to-3D contexts with a resampled MR/CT: 16 or
  * 32 (two 1024-thread CTAs per SM, patch radius 4 to 6; other radii take
  * it as 16); 0 = per launch (32 where it exists and the launch has four
  * CTAs per SM or more). No counterpart in the

@@ -231,6 +231,7 @@ struct lc2_context {
     int count;
     cudaGraph_t graph;
     cudaGraphExec_t exec;
+    long long kernels;  // kernel launches in the graph
   };
   std::vector<Graph> graphs;
   bool use_graphs = true;
@@ -614,17 +615,17 @@ int launch_group_generic(lc2_context* c, int k0, int cnt, float* osig, float* om
 }
 
 // Output rows per tile of the fused kernels: the option if set, else 24 for
-// the 3D kernel of a resampled MR/CT with patch radius 3 or 4 (one 768-thread
-// CTA per SM: the fastest measured at 96^3 to 256^3, for one transform or
-// 512; at radius 2 16-row tiles were faster), 0 (per launch) in 2D, else 16.
+// the 3D kernels of a resampled MR/CT -- on presampled images at patch
+// radius 1-4 (k_fused_pt: 24 warps per SM against 16, 255 against 262 ms
+// for 512 transforms at 256^3), resampling in place at radius 3 or 4 (one
+// 768-thread CTA per SM) -- 0 (per launch) in 2D, else 16.
 int tile_rows(const lc2_context* c) {
   if (c->tile_rows > 0) return c->tile_rows;
   if (c->lc2_nd == 2) return 0;  // chosen per launch: 32 rows for large launches, else 16
   const int r = c->cfg.patch_size;
-  // 24-row tiles (768 threads) pay where the fused kernel gathers; on
-  // presampled images the 16-row tiles (123 registers, no spills) are faster
-  return (c->lc2_nd == 3 && c->cfg.high_res_is_moving && !c->presample && (r == 3 || r == 4))
-             ? 24 : 16;
+  if (c->lc2_nd != 3 || !c->cfg.high_res_is_moving) return 16;
+  if (c->presample) return r <= 4 ? 24 : 16;
+  return (r == 3 || r == 4) ? 24 : 16;
 }
 
 // The fused kernel (static ultrasound): one launch for `cnt` transforms.
@@ -689,36 +690,37 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
     // resample pass, then the fused kernel on the presampled images, in
     // groups of the presample buffer's capacity
     LC2_TRY(ensure_presample(c, cnt));
+    auto presample = [&](int j, int n, float* buf) {
+      const cudaStream_t st = c->stream;
+      if (c->cfg.storage == LC2_STORE_F16)
+        return lc2::presample_launch<__half>(c->d_moving, c->fp, c->d_xf, k0 + j, n, buf, st);
+      if (c->cfg.storage == LC2_STORE_BF16)
+        return lc2::presample_launch<__nv_bfloat16>(c->d_moving, c->fp, c->d_xf, k0 + j, n, buf,
+                                                    st);
+      return lc2::presample_launch<float>(c->d_moving, c->fp, c->d_xf, k0 + j, n, buf, st);
+    };
+    auto moments = [&](int j, int n, const float* buf) {
+      L.k0 = k0 + j;
+      L.cnt = n;
+      L.pre = buf;
+      // radius <= 4: the moments pass with the in-kernel Sobel on
+      // double-buffered limb planes
+      if (c->cfg.patch_size > 4) return fused();
+      if (c->cfg.storage == LC2_STORE_F16) return lc2::fused_ps_entry<__half>(L, buf);
+      if (c->cfg.storage == LC2_STORE_BF16) return lc2::fused_ps_entry<__nv_bfloat16>(L, buf);
+      return lc2::fused_ps_entry<float>(L, buf);
+    };
     for (int j = 0; j < cnt; j += c->pre_slots) {
       const int n = std::min(c->pre_slots, cnt - j);
       {
         TimerScope ts(c, K_WARP);
-        if (c->cfg.storage == LC2_STORE_F16)
-          e = lc2::presample_launch<__half>(c->d_moving, c->fp, c->d_xf, k0 + j, n, c->d_pre, c->stream);
-        else if (c->cfg.storage == LC2_STORE_BF16)
-          e = lc2::presample_launch<__nv_bfloat16>(c->d_moving, c->fp, c->d_xf, k0 + j, n, c->d_pre,
-                                                   c->stream);
-        else
-          e = lc2::presample_launch<float>(c->d_moving, c->fp, c->d_xf, k0 + j, n, c->d_pre, c->stream);
+        e = presample(j, n, c->d_pre);
       }
       ++c->launches;
       LC2_CUDA(e);
-      L.k0 = k0 + j;
-      L.cnt = n;
       {
-        L.pre = c->d_pre;
         TimerScope ts(c, K_MOMENTS);
-        if (c->cfg.patch_size <= 4) {
-          // the moments pass with the in-kernel Sobel on double-buffered limb planes
-          if (c->cfg.storage == LC2_STORE_F16)
-            e = lc2::fused_ps_entry<__half>(L, c->d_pre);
-          else if (c->cfg.storage == LC2_STORE_BF16)
-            e = lc2::fused_ps_entry<__nv_bfloat16>(L, c->d_pre);
-          else
-            e = lc2::fused_ps_entry<float>(L, c->d_pre);
-        } else {
-          e = fused();
-        }
+        e = moments(j, n, c->d_pre);
       }
       ++c->launches;
       LC2_CUDA(e);
@@ -1669,6 +1671,7 @@ int launch_batch_graph(lc2_context* c, int count) {
     int st = enqueue_batch(c, count);
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    const long long kernels = c->launches - before;
     c->launches = before;  // counted when the graph runs
     if (st != LC2_OK) {
       if (graph) cudaGraphDestroy(graph);
@@ -1681,13 +1684,11 @@ int launch_batch_graph(lc2_context* c, int count) {
       cudaGraphDestroy(graph);
       LC2_CUDA(e);
     }
-    c->graphs.push_back({count, graph, exec});
+    c->graphs.push_back({count, graph, exec, kernels});
     g = &c->graphs.back();
   }
   LC2_CUDA(cudaGraphLaunch(g->exec, c->stream));
-  c->launches += c->mi ? 2 * ((count + std::max(1, 65535 / c->virt.dim[2]) - 1) /
-                              std::max(1, 65535 / c->virt.dim[2])) + 1
-                       : 2;  // kernels in the graph
+  c->launches += g->kernels;
   ++c->graph_launches;
   return LC2_OK;
 }

@@ -230,3 +230,26 @@ def test_presample_fixed_modality(r, storage):
     for k in (0, 8):
         want = oracle_eval(case, mats[k], storage=storage)
         assert abs(ref[k] / want - 1.0) < 1e-5, (k, ref[k], want)
+
+
+def test_graph_replay_counts_its_kernels():
+    """A graph replay adds to lc2_launch_count the kernels that the same calls
+    issue one by one (with the presampled form: resample pass, moments pass
+    and the finalizing kernel), not a fixed count per graph."""
+    case = synth.case_3d(seed=82, mr_size=48, us_size=40, r=2, blobs=6)
+    ctx = make_context(case)
+    rng = np.random.default_rng(2)
+    mats = perturbed(case, rng, 11)
+    ctx.set_option(capi.OPTION_GRAPHS, 0)
+    n0 = ctx.launch_count()
+    ref = ctx.evaluate_batch(mats)
+    direct = ctx.launch_count() - n0
+    assert direct >= 3
+    ctx.set_option(capi.OPTION_GRAPHS, 1)
+    np.testing.assert_array_equal(ctx.evaluate_batch(mats), ref)  # captures, then replays
+    n0 = ctx.launch_count()
+    g0 = ctx.graph_launches()
+    np.testing.assert_array_equal(ctx.evaluate_batch(mats), ref)
+    assert ctx.graph_launches() == g0 + 1
+    assert ctx.launch_count() - n0 == direct
+    ctx.close()
