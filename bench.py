@@ -792,19 +792,21 @@ def main():
     traffic = None
     ipv = None  # thread instructions per output voxel of the fused kernel (ncu)
     captured = None
+    # the moments kernel of the tuned launch: 24-row tiles run k_fused_pt,
+    # 8- and 16-row tiles k_fused_ps (presampled 3D form, radius <= 4)
+    kname = "k_fused_pt" if tuned[0] == 24 else "k_fused_ps"
     tfile = os.path.join(ROOT, "profiles", "k_fused_traffic.json")
-    if os.path.exists(tfile):
+    if os.path.exists(tfile) and args.patch <= 4:
         try:
-            tj = json.load(open(tfile))
+            tj = json.load(open(tfile))["kernels"][kname]
             # DRAM bytes of the moments pass over the step's launches: it reads
             # each transform's presampled image, so it scales with K
-            per_t = tj.get("dram_bytes_per_transform")
-            traffic = int(per_t * K) if per_t else tj.get("bytes_per_launch_scaled")
+            traffic = int(tj["dram_bytes_per_transform"] * K)
             ipv = tj.get("thread_instructions_per_voxel")
             captured = tj.get("captured_at")
         except Exception:
             traffic = None
-    from_profile = ("from profiles/k_fused_traffic.json (ncu capture of the kernel"
+    from_profile = (f"from profiles/k_fused_traffic.json (ncu capture of {kname}"
                     + (f", {captured})" if captured else ")"))
 
     # ---- e2e through the public call, host buffers ----
@@ -874,7 +876,7 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "traffic_source": from_profile,
-                         "kernel": "k_fused_ps (moments pass; the resample pass is kernels_ms_per_step.warp)",
+                         "kernel": f"{kname} (moments pass; the resample pass is kernels_ms_per_step.warp)",
                          "launches_per_step": mom_launches,
                          "kernel_ms_per_launch": mom_ms / max(1, mom_launches),
                          "scope": "achieved and traffic are totals of the step's moments launches",

@@ -157,8 +157,9 @@ long long lc2_launch_count(const lc2_context* ctx);
  * tile of the fused 3D kernel: 16 (one CTA per SM), 24 (one 768-thread CTA
  * per SM; resampled MR/CT only, the resampled-ultrasound kernel takes it as
  * 16) or 8 (two per SM); 0 = automatic (for a resampled MR/CT 24 at patch
- * radius 1-4 on presampled images and at radius 3 or 4 when the kernel
- * resamples itself, LC2_OPTION_PRESAMPLE 0; else 16). On presampled images
+ * radius 1-4 on presampled images of grids of 8 M voxels or more and at
+ * radius 3 or 4 when the kernel resamples itself, LC2_OPTION_PRESAMPLE 0;
+ * else 16). On presampled images
  * at radius 1-4, 24 selects the 768-thread moments kernel and 8 or 16 the
  * 512-thread one. 2D and 2D-to-3D contexts with a resampled MR/CT: 16 or
  * 32 (two 1024-thread CTAs per SM, patch radius 4 to 6; other radii take

@@ -614,17 +614,19 @@ int launch_group_generic(lc2_context* c, int k0, int cnt, float* osig, float* om
                               cnt, osig, omeas);
 }
 
-// Output rows per tile of the fused kernels: the option if set, else 24 for
-// the 3D kernels of a resampled MR/CT -- on presampled images at patch
-// radius 1-4 (k_fused_pt: 24 warps per SM against 16, 255 against 262 ms
-// for 512 transforms at 256^3), resampling in place at radius 3 or 4 (one
-// 768-thread CTA per SM) -- 0 (per launch) in 2D, else 16.
+// Output rows per tile of the fused kernels: the option if set; in 2D 0 (per
+// launch); for the 3D kernels of a resampled MR/CT 24 -- on presampled
+// images at patch radius 1-4 for grids of 8 M voxels or more (k_fused_pt,
+// 24 warps per SM: at 256^3 2-3 % faster batched and 15 % for one transform
+// than 16-row tiles; on 96^3 grids 4-9 % slower batched, where fewer, taller
+// tiles split z into shorter chunks), resampling in place at radius 3 or 4
+// (one 768-thread CTA per SM) -- else 16.
 int tile_rows(const lc2_context* c) {
   if (c->tile_rows > 0) return c->tile_rows;
   if (c->lc2_nd == 2) return 0;  // chosen per launch: 32 rows for large launches, else 16
   const int r = c->cfg.patch_size;
   if (c->lc2_nd != 3 || !c->cfg.high_res_is_moving) return 16;
-  if (c->presample) return r <= 4 ? 24 : 16;
+  if (c->presample) return (r <= 4 && c->nv >= 8000000) ? 24 : 16;
   return (r == 3 || r == 4) ? 24 : 16;
 }
 
