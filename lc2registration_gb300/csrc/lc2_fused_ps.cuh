@@ -272,7 +272,12 @@ struct PtGeom {
   static constexpr int RING = 2 * R + 1;          // leaving qG of the z window
   static constexpr size_t PA = (size_t)HY * HXP;  // ints per limb plane
   static constexpr int PW = HX + 2, PH = HY + 2;  // presampled region with the Sobel margin
-  static constexpr int NPW = PW * PH;
+  // plane row pitch = 4 mod 8 words: the 8 x 4 tail blocks of halo points
+  // (rows two apart) read the float2 (Sz, Dz) plane without bank conflicts;
+  // the planes are written row by row over the full pitch (the PWP - PW
+  // padding columns hold zeros and are never read)
+  static constexpr int PWP = PW + (12 - PW % 8) % 8;
+  static constexpr int NPW = PWP * PH;
   static constexpr int WP = (NPW + NT - 1) / NT;
   static constexpr int XJOBS = kLimbs * HY * 4;   // (limb, row, quarter) of the x pass
   static constexpr int YJOBS = kLimbs * 32 * 4;   // (limb, column, quarter) of the y pass
@@ -283,7 +288,7 @@ struct PtGeom {
   static constexpr size_t OFF_S = OFF_LV + sizeof(int) * (size_t)RING * NP;
   static constexpr size_t OFF_A = OFF_S + (sizeof(long long) * 5 + sizeof(int) * 2) * (size_t)NS;
   static constexpr size_t BYTES = OFF_A + 2 * sizeof(int) * kLimbs * PA;
-  static_assert(NPW % 2 == 0, "the (Sz, Dz) plane follows the M plane");
+  static_assert(NPW % 2 == 0 && PWP % 8 == 4, "the (Sz, Dz) plane follows the M plane");
   static_assert(NS > 0 && NS <= NT, "two halo points per thread at most");
   static_assert(XJOBS <= 2 * NT && YJOBS <= 2 * NT, "two jobs per thread in each pass");
   static_assert(TY % 4 == 0, "four row quarters");
@@ -291,6 +296,28 @@ struct PtGeom {
                 "16-byte loads of the last quarter row stay in the row");
   static_assert(R > 4 || BYTES + 1024 <= 227 * 1024, "one CTA's shared memory must fit an SM");
 };
+
+// Halo point p -> (row, column) of the tile's HY x HX halo: the first 32
+// columns row by row (a warp per row), then the 2R-column tail; at radius 4
+// a warp takes 8 tail columns of rows r, r+2, r+4, r+6, so that its limb
+// stores (row pitch 44 words) and Sobel reads hit distinct banks.
+template <int R>
+__device__ __forceinline__ void pt_halo_point(int p, int& hy, int& hx) {
+  if (p < 32 * (kPtTY + 2 * R)) {
+    hy = p >> 5;
+    hx = p & 31;
+  } else {
+    const int t = p - 32 * (kPtTY + 2 * R);
+    if (2 * R == 8) {
+      const int tw = t >> 5, lane = t & 31;
+      hy = (tw >> 1) * 8 + (tw & 1) + 2 * (lane >> 3);
+      hx = 32 + (lane & 7);
+    } else {
+      hy = t / (2 * R);
+      hx = 32 + (t - hy * (2 * R));
+    }
+  }
+}
 
 // x window pass in place on quarter rows: job (limb, row, quarter), the
 // four quarters of a row on neighbouring lanes of one warp, which all load
@@ -401,13 +428,15 @@ __global__ void __launch_bounds__(32 * kPtTY, 1)
   // keeps them out of the loop-carried registers
   auto roff = [&](int k) {
     const int i = tid + k * NT;
-    const int py = i / G::PW, px = i - py * G::PW;
+    const int py = i / G::PWP, px = i - py * G::PWP;
     const int gx = x0 - R - 1 + px, gy = y0 - R - 1 + py;
-    return (i < G::NPW && gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy) ? gy * P.vx + gx : -1;
+    return (i < G::NPW && px < G::PW && gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy)
+               ? gy * P.vx + gx : -1;
   };
   auto pu = [&](int j) {
     const int p = tid + j * NT;
-    const int hy = p / G::HX, hx = p - hy * G::HX;
+    int hy, hx;
+    pt_halo_point<R>(p, hy, hx);
     const int gx = x0 - R + hx, gy = y0 - R + hy;
     return (p < G::NP && gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy) ? gy * P.vx + gx : -1;
   };
@@ -507,10 +536,11 @@ __global__ void __launch_bounds__(32 * kPtTY, 1)
     // window (the leaving slice's out), the window's 12 limbs into plane A
     auto point = [&](int j, long long* ap, int* aq) {
       const int p = tid + j * NT;
-      const int hy = p / G::HX, hx = p - hy * G::HX;
-      const int c = (hy + 1) * G::PW + hx + 1;
+      int hy, hx;
+      pt_halo_point<R>(p, hy, hx);
+      const int c = (hy + 1) * G::PWP + hx + 1;
       const float m = mc[c];
-      const float g = fused_sobel_sd<G::PW>(SD, c);
+      const float g = fused_sobel_sd<G::PWP>(SD, c);
       const int qm = quant(m, P.qm), qg = quant(g, P.qg), qu = quant(u_nx[j], P.qu);
       if (leave) {
         const int qml = quant(ml_nx[j], P.qm), qgl = lg[p], qul = quant(ul_nx[j], P.qu);
