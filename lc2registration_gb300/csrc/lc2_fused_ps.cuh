@@ -256,8 +256,11 @@ cudaError_t fused_ps_launch_r(const FusedLaunch& L, const float* M) {
 // slice in the z ring; qM and qU of the leaving slice are the quantised
 // values of the same presampled and ultrasound voxels read again (from L2:
 // the slice entered 2R+1 slices earlier), so the window holds the same
-// integers. The x and y window passes run on quarter rows and quarter
-// columns, two jobs per thread in each (73 registers, no spills).
+// integers. The x window pass runs in place on quarter rows, the y pass on
+// quarter columns from the limb planes into a buffer of its own, which the
+// solve reads: one limb buffer suffices (the next slice's limbs are written
+// after every thread's y pass), and the y pass needs no warp-level ordering.
+// Two jobs per thread in each pass (70 registers, no spills).
 constexpr int kPtTY = 24;
 
 template <int R>
@@ -287,7 +290,8 @@ struct PtGeom {
   static constexpr int NS = NP - NT;
   static constexpr size_t OFF_S = OFF_LV + sizeof(int) * (size_t)RING * NP;
   static constexpr size_t OFF_A = OFF_S + (sizeof(long long) * 5 + sizeof(int) * 2) * (size_t)NS;
-  static constexpr size_t BYTES = OFF_A + 2 * sizeof(int) * kLimbs * PA;
+  static constexpr size_t OFF_Y = OFF_A + sizeof(int) * kLimbs * PA;
+  static constexpr size_t BYTES = OFF_Y + sizeof(int) * kLimbs * TY * 32;
   static_assert(NPW % 2 == 0 && PWP % 8 == 4, "the (Sz, Dz) plane follows the M plane");
   static_assert(NS > 0 && NS <= NT, "two halo points per thread at most");
   static_assert(XJOBS <= 2 * NT && YJOBS <= 2 * NT, "two jobs per thread in each pass");
@@ -362,41 +366,33 @@ __device__ __forceinline__ void pt_xpass(int* __restrict__ A) {
   }
 }
 
-// y window pass in place on quarter columns: job (limb, column group,
-// quarter, column), the four quarters of 8 columns in one warp (lane
-// 8r + c: rows 6r..6r+5 of column c), which all load before any stores
-// (quarter r reads rows 6r..6r+5+2R, which later quarters overwrite); two
-// jobs per thread.
+// y window pass from the x sums in A to Y (limb, row, column): job (limb,
+// quarter, column), two per thread.
 template <int R>
-__device__ __forceinline__ void pt_ypass(int* __restrict__ A) {
+__device__ __forceinline__ void pt_ypass(const int* __restrict__ A, int* __restrict__ Y) {
   using G = PtGeom<R>;
   constexpr int H = G::TY / 4;
   constexpr int NIN = H + G::W - 1;
 #pragma unroll
   for (int rep = 0; rep < 2; ++rep) {
     const int it = threadIdx.x + rep * G::NT;
-    const bool act = it < G::YJOBS;
-    const int L = it >> 7, grp = (it >> 5) & 3, lane = it & 31;
-    const int r = lane >> 3, col = 8 * grp + (lane & 7);
-    int* c = A + (size_t)(act ? L : 0) * G::PA + (size_t)(r * H) * G::HXP + col;
-    int v[NIN];
-    if (act) {
+    if (it < G::YJOBS) {
+      const int L = it >> 7, r = (it >> 5) & 3, col = it & 31;
+      const int* c = A + (size_t)L * G::PA + (size_t)(r * H) * G::HXP + col;
+      int* o = Y + (size_t)L * G::TY * 32 + (r * H) * 32 + col;
+      int v[NIN];
 #pragma unroll
       for (int i = 0; i < NIN; ++i) v[i] = c[i * G::HXP];
-    }
-    __syncwarp();
-    if (act) {
       int a = 0;
 #pragma unroll
       for (int i = 0; i < G::W; ++i) a += v[i];
-      c[0] = a;
+      o[0] = a;
 #pragma unroll
       for (int y = 1; y < H; ++y) {
         a += v[y + G::W - 1] - v[y - 1];
-        c[y * G::HXP] = a;
+        o[y * 32] = a;
       }
     }
-    __syncwarp();
   }
 }
 
@@ -415,7 +411,8 @@ __global__ void __launch_bounds__(32 * kPtTY, 1)
   int* lv = reinterpret_cast<int*>(smem_raw + G::OFF_LV);
   long long* sp = reinterpret_cast<long long*>(smem_raw + G::OFF_S);
   int* sq = reinterpret_cast<int*>(sp + 5 * G::NS);
-  int* A0 = reinterpret_cast<int*>(smem_raw + G::OFF_A);
+  int* A = reinterpret_cast<int*>(smem_raw + G::OFF_A);
+  int* Y = reinterpret_cast<int*>(smem_raw + G::OFF_Y);
   const int tid = threadIdx.x, slot = blockIdx.x, tile = blockIdx.y;
   const int x0 = (tile % P.ntx) * 32, y0 = (tile / P.ntx) * TY;
   const int ox = tid & 31, oy = tid >> 5;
@@ -524,13 +521,11 @@ __global__ void __launch_bounds__(32 * kPtTY, 1)
   load_sig(e0 - R);
   __syncthreads();
   long long acc_m = 0;
-  int buf = 0;
   for (int e = e0; e < ze + R; ++e) {
     const int z = e - R;
     const int l = e - 2 * R - 1;
     const bool out = (z >= zb);
     const bool leave = (l >= e0);
-    int* A = A0 + (size_t)buf * kLimbs * G::PA;
     int* lg = lv + ((e - e0) % G::RING) * G::NP;  // the leaving slice's slot
     // one halo point: the entering slice's quantised fields into the z
     // window (the leaving slice's out), the window's 12 limbs into plane A
@@ -599,22 +594,21 @@ __global__ void __launch_bounds__(32 * kPtTY, 1)
     load_m(e + 3, r2);
     __syncthreads();
     if (out) {
-      pt_ypass<R>(A);
+      pt_ypass<R>(A, Y);
       __syncthreads();
       const int x = x0 + ox, y = y0 + oy;
       if (x < P.vx && y < P.vy) {
         float m = 0.0f;
         if (sg > 0.0f) {
-          const int* a = A + oy * G::HXP + ox;
+          const int* a = Y + oy * 32 + ox;
           int L[kLimbs];
 #pragma unroll
-          for (int k = 0; k < kLimbs; ++k) L[k] = a[k * G::PA];
+          for (int k = 0; k < kLimbs; ++k) L[k] = a[k * TY * 32];
           m = fused_measure<3, R>(P, sg, sv, L);
           acc_m += __float2int_rn(m * P.sum_scale);
         }
         if (out_measure && slot == 0) out_measure[(size_t)z * slice + (size_t)y * P.vx + x] = m;
       }
-      buf ^= 1;
     }
   }
 #pragma unroll
