@@ -653,6 +653,40 @@ int ensure_presample(lc2_context* c, int count) {
   return LC2_OK;
 }
 
+// Transforms per presample group for a batch of cnt: at most the buffer's
+// slots, chosen so that the moments launches (one CTA per SM and tile) fill
+// whole waves of the device, by the launchers' z-split cost model -- waves x
+// (chunk + 2R + 3), summed over the groups; ties go to larger groups. At
+// 256^3 with 24-row tiles a transform has 88 tiles: groups of 19 fill 11
+// waves of 152 SMs exactly, where groups of 32 leave every 19th wave half
+// empty (297 against 304 waves for 512 transforms). Values do not depend on
+// the grouping.
+int presample_group(const lc2_context* c, int cnt, int ty) {
+  const int cap = c->pre_slots;
+  if (cnt <= cap) return cnt;
+  const int vz = c->virt.dim[2], r = c->cfg.patch_size;
+  const long long sms = std::max(1, c->sms);
+  const long long tiles =
+      (long long)((c->virt.dim[0] + 31) / 32) * ((c->virt.dim[1] + ty - 1) / ty);
+  auto cost = [&](int n) -> long long {
+    if (n <= 0) return 0;
+    const int zc = c->zchunk > 0 ? std::min(c->zchunk, vz)
+                                 : lc2::auto_zchunk(vz, r, tiles * n, sms);
+    const long long chunks = (vz + zc - 1) / zc;
+    return (tiles * n * chunks + sms - 1) / sms * (zc + 2 * r + 3);
+  };
+  int best_g = cap;
+  long long best = -1;
+  for (int g = cap; g >= (cap + 1) / 2; --g) {
+    const long long total = (long long)(cnt / g) * cost(g) + cost(cnt % g);
+    if (best < 0 || total < best) {
+      best = total;
+      best_g = g;
+    }
+  }
+  return best_g;
+}
+
 int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
   c->acc_clean = false;
   if (!c->cfg.high_res_is_moving || !c->d_sigma || !c->d_su)
@@ -712,8 +746,12 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
       if (c->cfg.storage == LC2_STORE_BF16) return lc2::fused_ps_entry<__nv_bfloat16>(L, buf);
       return lc2::fused_ps_entry<float>(L, buf);
     };
-    for (int j = 0; j < cnt; j += c->pre_slots) {
-      const int n = std::min(c->pre_slots, cnt - j);
+    // the moments kernel's tile height: 24 (k_fused_pt), 16 (k_fused_ps) or,
+    // beyond radius 4, 8 (k_fused on presampled images)
+    const int ty = c->cfg.patch_size > 4 ? 8 : (L.tile_height == 24 ? 24 : 16);
+    const int group = presample_group(c, cnt, ty);
+    for (int j = 0; j < cnt; j += group) {
+      const int n = std::min(group, cnt - j);
       {
         TimerScope ts(c, K_WARP);
         e = presample(j, n, c->d_pre);
