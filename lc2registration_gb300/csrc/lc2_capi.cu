@@ -654,18 +654,18 @@ int ensure_presample(lc2_context* c, int count) {
 }
 
 // Transforms per presample group for a batch of cnt: at most the buffer's
-// slots, chosen so that the moments launches (one CTA per SM and tile) fill
-// whole waves of the device, by the launchers' z-split cost model -- waves x
-// (chunk + 2R + 3), summed over the groups; ties go to larger groups. At
-// 256^3 with 24-row tiles a transform has 88 tiles: groups of 19 fill 11
-// waves of 152 SMs exactly, where groups of 32 leave every 19th wave half
-// empty (297 against 304 waves for 512 transforms). Values do not depend on
-// the grouping.
-int presample_group(const lc2_context* c, int cnt, int ty) {
+// slots, chosen so that the moments launches (tiles of ty rows, per_sm CTAs
+// resident per SM) fill whole waves of the device, by the launchers' z-split
+// cost model -- waves x (chunk + 2R + 3), summed over the groups; ties go to
+// larger groups. At 256^3 with 24-row tiles a transform has 88 tiles: groups
+// of 19 fill 11 waves of 152 SMs exactly, where groups of 32 leave every 19th
+// wave half empty (297 against 304 waves for 512 transforms). Values do not
+// depend on the grouping.
+int presample_group(const lc2_context* c, int cnt, int ty, int per_sm) {
   const int cap = c->pre_slots;
   if (cnt <= cap) return cnt;
   const int vz = c->virt.dim[2], r = c->cfg.patch_size;
-  const long long sms = std::max(1, c->sms);
+  const long long sms = (long long)std::max(1, c->sms) * std::max(1, per_sm);
   const long long tiles =
       (long long)((c->virt.dim[0] + 31) / 32) * ((c->virt.dim[1] + ty - 1) / ty);
   auto cost = [&](int n) -> long long {
@@ -749,7 +749,7 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
     // the moments kernel's tile height: 24 (k_fused_pt), 16 (k_fused_ps) or,
     // beyond radius 4, 8 (k_fused on presampled images)
     const int ty = c->cfg.patch_size > 4 ? 8 : (L.tile_height == 24 ? 24 : 16);
-    const int group = presample_group(c, cnt, ty);
+    const int group = presample_group(c, cnt, ty, 1);
     for (int j = 0; j < cnt; j += group) {
       const int n = std::min(group, cnt - j);
       {
@@ -814,8 +814,11 @@ int launch_fused_fixed(lc2_context* c, int k0, int cnt) {
     // the ultrasound resampled in a pass of its own, then the moments, in
     // groups of the presample buffer's capacity
     LC2_TRY(ensure_presample(c, cnt));
-    for (int j = 0; j < cnt; j += c->pre_slots) {
-      const int n = std::min(c->pre_slots, cnt - j);
+    // k_fused_fixed3's tile height and CTAs per SM
+    const int ty = (c->cfg.patch_size > 4 || L.tile_height == 8) ? 8 : 16;
+    const int group = presample_group(c, cnt, ty, lc2::fused_min_blocks(3, ty, c->cfg.patch_size));
+    for (int j = 0; j < cnt; j += group) {
+      const int n = std::min(group, cnt - j);
       {
         TimerScope ts(c, K_WARP);
         if (c->cfg.storage == LC2_STORE_F16)

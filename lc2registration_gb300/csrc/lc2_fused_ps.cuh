@@ -260,7 +260,7 @@ cudaError_t fused_ps_launch_r(const FusedLaunch& L, const float* M) {
 // quarter columns from the limb planes into a buffer of its own, which the
 // solve reads: one limb buffer suffices (the next slice's limbs are written
 // after every thread's y pass), and the y pass needs no warp-level ordering.
-// Two jobs per thread in each pass (70 registers, no spills).
+// Two jobs per thread in each pass (69 registers, no spills).
 constexpr int kPtTY = 24;
 
 template <int R>
@@ -421,22 +421,27 @@ __global__ void __launch_bounds__(32 * kPtTY, 1)
   const size_t slice = (size_t)P.vx * P.vy;
   const float* Ms = Mb + (size_t)slot * slice * P.vz;
   // offsets in a slice of the thread's region points (planes) and halo
-  // points (moments), -1 outside the grid; recomputed where used, which
-  // keeps them out of the loop-carried registers
-  auto roff = [&](int k) {
+  // points (moments), -1 outside the grid, and each halo point's index in the
+  // planes and in the limb planes
+  int ro[WP], po[MAXP], pc[MAXP], pa[MAXP];
+#pragma unroll
+  for (int k = 0; k < WP; ++k) {
     const int i = tid + k * NT;
     const int py = i / G::PWP, px = i - py * G::PWP;
     const int gx = x0 - R - 1 + px, gy = y0 - R - 1 + py;
-    return (i < G::NPW && px < G::PW && gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy)
-               ? gy * P.vx + gx : -1;
-  };
-  auto pu = [&](int j) {
+    ro[k] = (i < G::NPW && px < G::PW && gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy)
+                ? gy * P.vx + gx : -1;
+  }
+#pragma unroll
+  for (int j = 0; j < MAXP; ++j) {
     const int p = tid + j * NT;
     int hy, hx;
     pt_halo_point<R>(p, hy, hx);
     const int gx = x0 - R + hx, gy = y0 - R + hy;
-    return (p < G::NP && gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy) ? gy * P.vx + gx : -1;
-  };
+    po[j] = (p < G::NP && gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy) ? gy * P.vx + gx : -1;
+    pc[j] = (hy + 1) * G::PWP + hx + 1;
+    pa[j] = hy * G::HXP + hx;
+  }
   // z-window sums of the first halo point in registers, of the second in
   // shared memory
   int accq[2] = {0, 0};
@@ -453,7 +458,7 @@ __global__ void __launch_bounds__(32 * kPtTY, 1)
     const float* src = Ms + (size_t)(zin ? e : 0) * slice;
 #pragma unroll
     for (int k = 0; k < WP; ++k) {
-      const int o = roff(k);
+      const int o = ro[k];
       out[k] = (zin && o >= 0) ? __ldg(src + o) : 0.0f;
     }
   };
@@ -491,7 +496,7 @@ __global__ void __launch_bounds__(32 * kPtTY, 1)
     const bool lin = (l >= e0 && l >= 0 && l < P.vz);
 #pragma unroll
     for (int j = 0; j < MAXP; ++j) {
-      const int o = pu(j);
+      const int o = po[j];
       u_nx[j] = (zin && o >= 0) ? ldf(Ust, (size_t)e * slice + o) : 0.0f;
       ml_nx[j] = (lin && o >= 0) ? __ldcs(Ms + (size_t)l * slice + o) : 0.0f;
       ul_nx[j] = (lin && o >= 0) ? ldf(Ust, (size_t)l * slice + o) : 0.0f;
@@ -531,9 +536,7 @@ __global__ void __launch_bounds__(32 * kPtTY, 1)
     // window (the leaving slice's out), the window's 12 limbs into plane A
     auto point = [&](int j, long long* ap, int* aq) {
       const int p = tid + j * NT;
-      int hy, hx;
-      pt_halo_point<R>(p, hy, hx);
-      const int c = (hy + 1) * G::PWP + hx + 1;
+      const int c = pc[j];
       const float m = mc[c];
       const float g = fused_sobel_sd<G::PWP>(SD, c);
       const int qm = quant(m, P.qm), qg = quant(g, P.qg), qu = quant(u_nx[j], P.qu);
@@ -556,7 +559,7 @@ __global__ void __launch_bounds__(32 * kPtTY, 1)
       aq[0] += qm;
       aq[1] += qg;
       if (out) {
-        int* a = A + hy * G::HXP + hx;
+        int* a = A + pa[j];
         a[0] = aq[0];
         a[G::PA] = aq[1];
 #pragma unroll
