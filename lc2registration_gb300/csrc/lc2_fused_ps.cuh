@@ -256,11 +256,10 @@ cudaError_t fused_ps_launch_r(const FusedLaunch& L, const float* M) {
 // slice in the z ring; qM and qU of the leaving slice are the quantised
 // values of the same presampled and ultrasound voxels read again (from L2:
 // the slice entered 2R+1 slices earlier), so the window holds the same
-// integers. The x window pass runs in place on quarter rows, the y pass on
-// quarter columns from the limb planes into a buffer of its own, which the
-// solve reads: one limb buffer suffices (the next slice's limbs are written
-// after every thread's y pass), and the y pass needs no warp-level ordering.
-// Two jobs per thread in each pass (69 registers, no spills).
+// integers. The x window pass runs in place on quarter rows (two jobs per
+// thread), the y pass on whole columns from the limb planes into a buffer of
+// its own, which the solve reads: one limb buffer suffices (the next slice's
+// limbs are written after every thread's y pass). 80 registers, no spills.
 constexpr int kPtTY = 24;
 
 template <int R>
@@ -283,7 +282,7 @@ struct PtGeom {
   static constexpr int NPW = PWP * PH;
   static constexpr int WP = (NPW + NT - 1) / NT;
   static constexpr int XJOBS = kLimbs * HY * 4;   // (limb, row, quarter) of the x pass
-  static constexpr int YJOBS = kLimbs * 32 * 4;   // (limb, column, quarter) of the y pass
+  static constexpr int YJOBS = kLimbs * 32;       // (limb, column) of the y pass
   static constexpr size_t OFF_LV = ((sizeof(float) * 3 * (size_t)NPW + 15) / 16) * 16;
   // z-window sums of the halo points beyond the first NT (the second point
   // of threads < NS) live in shared memory: 5 products, then qM and qG
@@ -294,7 +293,7 @@ struct PtGeom {
   static constexpr size_t BYTES = OFF_Y + sizeof(int) * kLimbs * TY * 32;
   static_assert(NPW % 2 == 0 && PWP % 8 == 4, "the (Sz, Dz) plane follows the M plane");
   static_assert(NS > 0 && NS <= NT, "two halo points per thread at most");
-  static_assert(XJOBS <= 2 * NT && YJOBS <= 2 * NT, "two jobs per thread in each pass");
+  static_assert(XJOBS <= 2 * NT && YJOBS <= NT, "two x jobs and one y job per thread at most");
   static_assert(TY % 4 == 0, "four row quarters");
   static_assert(HXP % 4 == 0 && 24 + 4 * ((8 + W - 1 + 3) / 4) <= HXP,
                 "16-byte loads of the last quarter row stay in the row");
@@ -366,32 +365,31 @@ __device__ __forceinline__ void pt_xpass(int* __restrict__ A) {
   }
 }
 
-// y window pass from the x sums in A to Y (limb, row, column): job (limb,
-// quarter, column), two per thread.
+// y window pass from the x sums in A to Y (limb, row, column): one thread
+// per (limb, column), the whole column in registers. Out of place, so no
+// ordering between threads; fewer, longer jobs than in the x pass because
+// this pass is bound by shared-memory wavefronts (a column's 32 words for
+// its 24 sums).
 template <int R>
 __device__ __forceinline__ void pt_ypass(const int* __restrict__ A, int* __restrict__ Y) {
   using G = PtGeom<R>;
-  constexpr int H = G::TY / 4;
-  constexpr int NIN = H + G::W - 1;
+  constexpr int NIN = G::HY;
+  const int it = threadIdx.x;
+  if (it < G::YJOBS) {
+    const int L = it >> 5, col = it & 31;
+    const int* c = A + (size_t)L * G::PA + col;
+    int* o = Y + (size_t)L * G::TY * 32 + col;
+    int v[NIN];
 #pragma unroll
-  for (int rep = 0; rep < 2; ++rep) {
-    const int it = threadIdx.x + rep * G::NT;
-    if (it < G::YJOBS) {
-      const int L = it >> 7, r = (it >> 5) & 3, col = it & 31;
-      const int* c = A + (size_t)L * G::PA + (size_t)(r * H) * G::HXP + col;
-      int* o = Y + (size_t)L * G::TY * 32 + (r * H) * 32 + col;
-      int v[NIN];
+    for (int i = 0; i < NIN; ++i) v[i] = c[i * G::HXP];
+    int a = 0;
 #pragma unroll
-      for (int i = 0; i < NIN; ++i) v[i] = c[i * G::HXP];
-      int a = 0;
+    for (int i = 0; i < G::W; ++i) a += v[i];
+    o[0] = a;
 #pragma unroll
-      for (int i = 0; i < G::W; ++i) a += v[i];
-      o[0] = a;
-#pragma unroll
-      for (int y = 1; y < H; ++y) {
-        a += v[y + G::W - 1] - v[y - 1];
-        o[y * 32] = a;
-      }
+    for (int y = 1; y < G::TY; ++y) {
+      a += v[y + G::W - 1] - v[y - 1];
+      o[y * 32] = a;
     }
   }
 }
