@@ -103,6 +103,31 @@ struct FusedGeom {
                 "one CTA's shared memory must fit an SM");
 };
 
+// Halo point p -> (row, column) of the HY x HX halo of a 3D tile of TY rows:
+// the first 32 columns row by row (a warp per row), then the 2R-column
+// tail; at radius 4 a warp takes 8 tail columns of rows r, r+2, r+4, r+6, so
+// that its stores to limb planes of row pitch 44 words (and its reads of a
+// float2 plane of pitch 4 mod 8 words) hit distinct banks.
+template <int TY, int R>
+__device__ __forceinline__ void halo_point(int p, int& hy, int& hx) {
+  constexpr int HY = TY + 2 * R;
+  static_assert(2 * R != 8 || HY % 8 == 0, "8-row groups of tail blocks");
+  if (p < 32 * HY) {
+    hy = p >> 5;
+    hx = p & 31;
+  } else {
+    const int t = p - 32 * HY;
+    if (2 * R == 8) {
+      const int tw = t >> 5, lane = t & 31;
+      hy = (tw >> 1) * 8 + (tw & 1) + 2 * (lane >> 3);
+      hx = 32 + (lane & 7);
+    } else {
+      hy = t / (2 * R);
+      hx = 32 + (t - hy * (2 * R));
+    }
+  }
+}
+
 // Halo point q of a 2D tile -> (hy, hx): the first 32 columns row by row,
 // one row per warp, then the 2R-column tail row by row. A warp's plane reads
 // and limb writes are then 32 consecutive words (row-major numbering over the

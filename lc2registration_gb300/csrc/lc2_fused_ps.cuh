@@ -300,28 +300,6 @@ struct PtGeom {
   static_assert(R > 4 || BYTES + 1024 <= 227 * 1024, "one CTA's shared memory must fit an SM");
 };
 
-// Halo point p -> (row, column) of the tile's HY x HX halo: the first 32
-// columns row by row (a warp per row), then the 2R-column tail; at radius 4
-// a warp takes 8 tail columns of rows r, r+2, r+4, r+6, so that its limb
-// stores (row pitch 44 words) and Sobel reads hit distinct banks.
-template <int R>
-__device__ __forceinline__ void pt_halo_point(int p, int& hy, int& hx) {
-  if (p < 32 * (kPtTY + 2 * R)) {
-    hy = p >> 5;
-    hx = p & 31;
-  } else {
-    const int t = p - 32 * (kPtTY + 2 * R);
-    if (2 * R == 8) {
-      const int tw = t >> 5, lane = t & 31;
-      hy = (tw >> 1) * 8 + (tw & 1) + 2 * (lane >> 3);
-      hx = 32 + (lane & 7);
-    } else {
-      hy = t / (2 * R);
-      hx = 32 + (t - hy * (2 * R));
-    }
-  }
-}
-
 // x window pass in place on quarter rows: job (limb, row, quarter), the
 // four quarters of a row on neighbouring lanes of one warp, which all load
 // before any stores (quarter q reads columns 8q..8q+7+2R, of which the next
@@ -434,7 +412,7 @@ __global__ void __launch_bounds__(32 * kPtTY, 1)
   for (int j = 0; j < MAXP; ++j) {
     const int p = tid + j * NT;
     int hy, hx;
-    pt_halo_point<R>(p, hy, hx);
+    halo_point<kPtTY, R>(p, hy, hx);
     const int gx = x0 - R + hx, gy = y0 - R + hy;
     po[j] = (p < G::NP && gx >= 0 && gx < P.vx && gy >= 0 && gy < P.vy) ? gy * P.vx + gx : -1;
     pc[j] = (hy + 1) * G::PWP + hx + 1;

@@ -253,3 +253,27 @@ def test_graph_replay_counts_its_kernels():
     assert ctx.graph_launches() == g0 + 1
     assert ctx.launch_count() - n0 == direct
     ctx.close()
+
+
+@pytest.mark.parametrize("hr_moving", [True, False])
+def test_presample_groups_do_not_change_values(hr_moving):
+    """A batch larger than the presample buffer (64 slots at this size) runs
+    as several groups, sized to fill whole waves of the device; every
+    transform's value equals its value in a batch of one group, bit for bit,
+    for both HighResolutionModality settings."""
+    base = synth.case_3d(seed=90, mr_size=40, us_size=32, r=2, blobs=5)
+    if hr_moving:
+        case = base
+        mats = perturbed(case, np.random.default_rng(5), 150)
+    else:
+        inv = np.linalg.inv(base.true_mat.astype(np.float64)).astype(np.float32)
+        case = synth.Case(base.mode, base.moving_geom, base.moving, base.fixed_geom, base.fixed,
+                          [1.0, 1.0, 1.0], 2, hr_moving=False, true_params={}, true_mat=inv)
+        mats = np.linalg.inv(perturbed(base, np.random.default_rng(5), 150).astype(np.float64))
+        mats = mats.astype(np.float32)
+    ctx = make_context(case)
+    whole = ctx.evaluate_batch(mats)
+    parts = np.concatenate([ctx.evaluate_batch(mats[i:i + 50]) for i in range(0, 150, 50)])
+    np.testing.assert_array_equal(whole, parts)
+    np.testing.assert_array_equal([ctx.evaluate(mats[k]) for k in (0, 77, 149)], whole[[0, 77, 149]])
+    ctx.close()
