@@ -661,19 +661,31 @@ int ensure_presample(lc2_context* c, int count) {
 // of 19 fill 11 waves of 152 SMs exactly, where groups of 32 leave every 19th
 // wave half empty (297 against 304 waves for 512 transforms). Values do not
 // depend on the grouping.
+// Rows of the grid that 24-row tiles leave over, run as one row of 16-row
+// tiles when they fit in it (1-16 rows): at 256 rows, 10 tiles of 24 and one
+// of 16 instead of 11 of 24 (3 % of the rows computed outside the grid).
+int pt_rest_rows(const lc2_context* c) {
+  const int vy = c->virt.dim[1], rest = vy % 24;
+  return (vy > 24 && rest > 0 && rest <= 16) ? rest : 0;
+}
+
 int presample_group(const lc2_context* c, int cnt, int ty, int per_sm) {
   const int cap = c->pre_slots;
   if (cnt <= cap) return cnt;
   const int vz = c->virt.dim[2], r = c->cfg.patch_size;
   const long long sms = (long long)std::max(1, c->sms) * std::max(1, per_sm);
-  const long long tiles =
-      (long long)((c->virt.dim[0] + 31) / 32) * ((c->virt.dim[1] + ty - 1) / ty);
+  const long long ntx = (c->virt.dim[0] + 31) / 32;
+  // launches per group: (tiles per transform, weight = tile rows)
+  const int rest = ty == 24 ? pt_rest_rows(c) : 0;
+  const long long tiles = ntx * ((c->virt.dim[1] - rest + ty - 1) / ty);
+  auto launch_cost = [&](long long t, int n) -> long long {
+    const int zc = c->zchunk > 0 ? std::min(c->zchunk, vz) : lc2::auto_zchunk(vz, r, t * n, sms);
+    const long long chunks = (vz + zc - 1) / zc;
+    return (t * n * chunks + sms - 1) / sms * (zc + 2 * r + 3);
+  };
   auto cost = [&](int n) -> long long {
     if (n <= 0) return 0;
-    const int zc = c->zchunk > 0 ? std::min(c->zchunk, vz)
-                                 : lc2::auto_zchunk(vz, r, tiles * n, sms);
-    const long long chunks = (vz + zc - 1) / zc;
-    return (tiles * n * chunks + sms - 1) / sms * (zc + 2 * r + 3);
+    return launch_cost(tiles, n) * ty + (rest ? launch_cost(ntx, n) * 16 : 0);
   };
   int best_g = cap;
   long long best = -1;
@@ -735,16 +747,37 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
                                                     st);
       return lc2::presample_launch<float>(c->d_moving, c->fp, c->d_xf, k0 + j, n, buf, st);
     };
+    auto moments_one = [&](const float* buf) {
+      if (c->cfg.storage == LC2_STORE_F16) return lc2::fused_ps_entry<__half>(L, buf);
+      if (c->cfg.storage == LC2_STORE_BF16) return lc2::fused_ps_entry<__nv_bfloat16>(L, buf);
+      return lc2::fused_ps_entry<float>(L, buf);
+    };
+    // the moments pass of a group: radius <= 4 with the in-kernel Sobel
+    // (k_fused_pt on 24-row tiles, the rows left over by them as one row
+    // of k_fused_ps tiles; k_fused_ps on 8/16-row tiles), else k_fused
     auto moments = [&](int j, int n, const float* buf) {
       L.k0 = k0 + j;
       L.cnt = n;
       L.pre = buf;
-      // radius <= 4: the moments pass with the in-kernel Sobel on
-      // double-buffered limb planes
-      if (c->cfg.patch_size > 4) return fused();
-      if (c->cfg.storage == LC2_STORE_F16) return lc2::fused_ps_entry<__half>(L, buf);
-      if (c->cfg.storage == LC2_STORE_BF16) return lc2::fused_ps_entry<__nv_bfloat16>(L, buf);
-      return lc2::fused_ps_entry<float>(L, buf);
+      if (c->cfg.patch_size > 4) {
+        ++c->launches;
+        return fused();
+      }
+      const int rest = L.tile_height == 24 ? pt_rest_rows(c) : 0;
+      L.y_off = 0;
+      L.y_rows = c->virt.dim[1] - rest;
+      cudaError_t err = moments_one(buf);
+      ++c->launches;
+      if (err == cudaSuccess && rest) {
+        L.tile_height = 16;
+        L.y_off = c->virt.dim[1] - rest;
+        L.y_rows = rest;
+        err = moments_one(buf);
+        ++c->launches;
+        L.tile_height = 24;
+      }
+      L.y_off = L.y_rows = 0;
+      return err;
     };
     // the moments kernel's tile height: 24 (k_fused_pt), 16 (k_fused_ps) or,
     // beyond radius 4, 8 (k_fused on presampled images)
@@ -762,7 +795,6 @@ int launch_fused(lc2_context* c, int k0, int cnt, float* omeas) {
         TimerScope ts(c, K_MOMENTS);
         e = moments(j, n, c->d_pre);
       }
-      ++c->launches;
       LC2_CUDA(e);
     }
     return LC2_OK;

@@ -43,6 +43,7 @@ struct FusedParams {
   long long thr_var;       // valid-patch variance threshold (resampled ultrasound)
   float sig_scale;         // sigma = sqrt(D_uu) * sig_scale
   float sum_scale;         // fixed-point scale of the measure sum
+  int y0;                  // first output row of the launch's tiles (presampled 3D kernels)
 };
 
 constexpr int kLimbs = 12;
@@ -984,6 +985,9 @@ struct FusedLaunch {
   int sms;          // multiprocessors of the device
   cudaStream_t stream;
   const float* pre = nullptr;  // 3D: presampled moving image of the launch (k_presample)
+  // presampled 3D kernels: the launch's tiles cover output rows [y_off,
+  // y_off + y_rows) (y_rows 0: the whole grid)
+  int y_off = 0, y_rows = 0;
 };
 
 template <int ND, int WND, typename T, int R, int TY, typename K>

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(32 * kPsTY, 1)
   int* lv = reinterpret_cast<int*>(smem_raw + G::OFF_LV);
   int* A0 = reinterpret_cast<int*>(smem_raw + G::OFF_A);
   const int tid = threadIdx.x, slot = blockIdx.x, tile = blockIdx.y;
-  const int x0 = (tile % P.ntx) * 32, y0 = (tile / P.ntx) * TY;
+  const int x0 = (tile % P.ntx) * 32, y0 = P.y0 + (tile / P.ntx) * TY;
   const int ox = tid & 31, oy = tid >> 5;
   const int zb = blockIdx.z * P.zchunk;
   const int ze = min(zb + P.zchunk, P.vz);
@@ -238,8 +238,10 @@ cudaError_t fused_ps_launch_r(const FusedLaunch& L, const float* M) {
                                        (int)G::BYTES);
   if (e != cudaSuccess) return e;
   FusedParams P = L.P;
-  const int ntx = (P.vx + 31) / 32, nty = (P.vy + G::TY - 1) / G::TY;
+  const int rows = L.y_rows > 0 ? L.y_rows : P.vy;
+  const int ntx = (P.vx + 31) / 32, nty = (rows + G::TY - 1) / G::TY;
   P.ntx = ntx;
+  P.y0 = L.y_off;
   if (L.zchunk > 0)
     P.zchunk = L.zchunk < P.vz ? L.zchunk : P.vz;
   else
@@ -390,7 +392,7 @@ __global__ void __launch_bounds__(32 * kPtTY, 1)
   int* A = reinterpret_cast<int*>(smem_raw + G::OFF_A);
   int* Y = reinterpret_cast<int*>(smem_raw + G::OFF_Y);
   const int tid = threadIdx.x, slot = blockIdx.x, tile = blockIdx.y;
-  const int x0 = (tile % P.ntx) * 32, y0 = (tile / P.ntx) * TY;
+  const int x0 = (tile % P.ntx) * 32, y0 = P.y0 + (tile / P.ntx) * TY;
   const int ox = tid & 31, oy = tid >> 5;
   const int zb = blockIdx.z * P.zchunk;
   const int ze = min(zb + P.zchunk, P.vz);
@@ -605,8 +607,10 @@ cudaError_t fused_pt_launch_r(const FusedLaunch& L, const float* M) {
                                        (int)G::BYTES);
   if (e != cudaSuccess) return e;
   FusedParams P = L.P;
-  const int ntx = (P.vx + 31) / 32, nty = (P.vy + G::TY - 1) / G::TY;
+  const int rows = L.y_rows > 0 ? L.y_rows : P.vy;
+  const int ntx = (P.vx + 31) / 32, nty = (rows + G::TY - 1) / G::TY;
   P.ntx = ntx;
+  P.y0 = L.y_off;
   if (L.zchunk > 0)
     P.zchunk = L.zchunk < P.vz ? L.zchunk : P.vz;
   else
