@@ -203,8 +203,9 @@ struct lc2_context {
   // and its Sobel quantised, their window sums and centred sums
   // (lc2_fused_fixed.cuh)
   int* d_fq = nullptr;
-  int* d_fs = nullptr;
+  int* d_fs = nullptr;        // (S_M, S_G) per voxel, interleaved
   long long* d_fd = nullptr;
+  float4* d_fsv = nullptr;    // solve factors per voxel (k_fixed_solve_static)
   int generic = 0;  // LC2_OPTION_GENERIC
   int sms = 152;    // multiprocessors of the device (queried at creation)
   // normalised mutual information (patch_size 0): static image bins and
@@ -304,6 +305,24 @@ __global__ void k_fixed_centre(const int* __restrict__ s, long long* __restrict_
     d[i] = n * d[i] - sm * sm;
     d[nv + i] = n * d[nv + i] - sg * sg;
     d[2 * nv + i] = n * d[2 * nv + i] - sm * sg;
+  }
+}
+
+// Per static voxel: (S_M, S_G) interleaved, and the solve factors of
+// solve_centred_static -- im = rsqrtf(D_mm) when D_mm > thr_m else 0, ig
+// likewise, rmg = D_mg im ig when both columns count -- with the float
+// operations solve_centred applies to them.
+__global__ void k_fixed_solve_static(const int* __restrict__ s, const long long* __restrict__ d,
+                                     size_t nv, long long thr_m, long long thr_g,
+                                     int2* __restrict__ smg, float4* __restrict__ sv) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const long long dmm = d[i], dgg = d[nv + i], dmg = d[2 * nv + i];
+    const bool km = dmm > thr_m, kg = dgg > thr_g;
+    const float im = km ? rsqrtf(ll2f(dmm)) : 0.0f, ig = kg ? rsqrtf(ll2f(dgg)) : 0.0f;
+    const float rmg = (km && kg) ? ll2f(dmg) * im * ig : 0.0f;
+    smg[i] = make_int2(s[i], s[nv + i]);
+    sv[i] = make_float4(im, ig, rmg, 0.0f);
   }
 }
 
@@ -818,7 +837,8 @@ int launch_fused_fixed(lc2_context* c, int k0, int cnt) {
                 "HighResolutionModality: Fixed");
   lc2::FixedLaunch L;
   L.mov = c->d_moving;
-  L.S = lc2::FixedStatic{c->d_fq, c->d_fs, c->d_fd, c->nv};
+  L.S = lc2::FixedStatic{c->d_fq, reinterpret_cast<const int2*>(c->d_fs), c->d_fd, c->nv,
+                         c->d_fsv};
   L.P = c->fp;
   L.xf = c->d_xf;
   L.k0 = k0;
@@ -1070,7 +1090,8 @@ void context_bytes(const lc2_context* c, size_t* held, size_t* peak_extra) {
   h += c->nv * (hrm ? es : sizeof(float));     // static image on the virtual grid
   if (!hrm) h += c->nv * sizeof(float);        // its Sobel
   if (hrm && !c->mi) h += c->nv * (sizeof(float) + sizeof(int));  // weighting factors, S_U
-  if (!hrm && !c->mi) h += c->nv * (4 * sizeof(int) + 3 * sizeof(long long));  // static sums
+  if (!hrm && !c->mi)  // static sums and solve factors
+    h += c->nv * (4 * sizeof(int) + 3 * sizeof(long long) + sizeof(float4));
   if (c->mi)
     h += c->nv + 64 * (sizeof(unsigned) * (lc2::kMiHist + 2) + sizeof(double) * 2 * lc2::kMiParts);
   h += 64 * (sizeof(lc2::Xform) + 2 * sizeof(unsigned long long) + sizeof(double));
@@ -1121,6 +1142,8 @@ int create_context(const lc2_config* cfg, bool own_moving, lc2_context** out) {
     e = dev_alloc((void**)&c->d_fs, 2 * c->nv * sizeof(int), c->stream);
   if (e == cudaSuccess && !cfg->high_res_is_moving && !c->mi)
     e = dev_alloc((void**)&c->d_fd, 3 * c->nv * sizeof(long long), c->stream);
+  if (e == cudaSuccess && !cfg->high_res_is_moving && !c->mi)
+    e = dev_alloc((void**)&c->d_fsv, c->nv * sizeof(float4), c->stream);
   if (e == cudaSuccess) e = dev_alloc((void**)&c->d_err, sizeof(int), c->stream);
   if (e == cudaSuccess) e = host_alloc((void**)&c->h_err, sizeof(int));
   if (e == cudaSuccess) *c->h_err = 0;  // pinned buffers come from a reuse cache
@@ -1178,6 +1201,7 @@ int lc2_destroy(lc2_context* c) {
   dev_free(c->d_fq, fs);
   dev_free(c->d_fs, fs);
   dev_free(c->d_fd, fs);
+  dev_free(c->d_fsv, fs);
   dev_free(c->d_err, fs);
   dev_free(c->d_scratch, fs);
   dev_free(c->d_sbin, fs);
@@ -1486,7 +1510,13 @@ int fixed_static_sums(lc2_context* c) {
     }
   }
   lc2::k_fixed_centre<<<blocks, 256, 0, c->stream>>>(c->d_fs, c->d_fd, nv, (long long)c->n);
-  c->launches += 2;
+  // the solve factors, and (S_M, S_G) interleaved per voxel through the
+  // 8-byte temporary into the sums' own buffer
+  lc2::k_fixed_solve_static<<<blocks, 256, 0, c->stream>>>(c->d_fs, c->d_fd, nv, c->fp.thr_m,
+                                                           c->fp.thr_g,
+                                                           reinterpret_cast<int2*>(tl), c->d_fsv);
+  LC2_CUDA(cudaMemcpyAsync(c->d_fs, tl, nv * sizeof(int2), cudaMemcpyDeviceToDevice, c->stream));
+  c->launches += 3;
   LC2_CUDA(cudaGetLastError());
   LC2_CUDA(cudaStreamSynchronize(c->stream));
   return LC2_OK;

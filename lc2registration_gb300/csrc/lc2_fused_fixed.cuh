@@ -29,9 +29,10 @@ namespace lc2 {
 // Static precomputed fields of the high-resolution image, per virtual voxel.
 struct FixedStatic {
   const int* q;        // quantised M, G: [2][nv]
-  const int* s;        // window sums S_M, S_G: [2][nv]
+  const int2* s;       // window sums (S_M, S_G) per voxel: [nv]
   const long long* d;  // centred sums D_mm, D_gg, D_mg: [3][nv]
   size_t nv;
+  const float4* sv;    // solve factors (im, ig, rmg, 0) per voxel (solve_centred_static)
 };
 
 // Limbs: S_U, invalid count, then (lo, hi) of UU, UM and UG.
@@ -76,13 +77,13 @@ __device__ __forceinline__ void fixed_solve(const FusedParams& P, const FixedSta
   const long long uu = (long long)a[3 * ls] * (1LL << K) + a[2 * ls];
   const long long um = (long long)a[5 * ls] * (1LL << K) + a[4 * ls];
   const long long ug = (long long)a[7 * ls] * (1LL << K) + a[6 * ls];
-  const int sm = __ldg(S.s + gi), sg = __ldg(S.s + S.nv + gi);
-  const long long dmm = __ldg(S.d + gi), dgg = __ldg(S.d + S.nv + gi),
-                  dmg = __ldg(S.d + 2 * S.nv + gi);
+  const int2 smg = __ldg(S.s + gi);
+  const float4 sv = __ldg(S.sv + gi);
   constexpr long long n = PatchConst<ND, R>::N;
   float sigma, m;
-  solve_centred(n * uu - (long long)su * su, dmm, dgg, dmg, n * um - (long long)su * sm,
-                n * ug - (long long)su * sg, P.thr_var, P.thr_m, P.thr_g, P.sig_scale, sigma, m);
+  solve_centred_static(n * uu - (long long)su * su, n * um - (long long)su * smg.x,
+                       n * ug - (long long)su * smg.y, sv, S.d, S.nv, gi, P.thr_var,
+                       P.sig_scale, sigma, m);
   acc_m += __float2int_rn(m * P.sum_scale);
   acc_s += __float2int_rn(sigma * P.sum_scale);
 }
@@ -171,17 +172,14 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
   }
   long long acc_m = 0, acc_s = 0;
   // static fields of the next output voxel solved, loaded a slice ahead
-  int nsm = 0, nsg = 0;
-  long long ndmm = 0, ndgg = 0, ndmg = 0;
+  int2 nsmg = make_int2(0, 0);
+  float4 nsv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   auto load_static = [&](int z) {
     const int x = x0 + ox, y = y0 + oy;
     if (z >= zb && z < ze && x < P.vx && y < P.vy) {
       const size_t gi = ((size_t)z * P.vy + y) * P.vx + x;
-      nsm = __ldg(S.s + gi);
-      nsg = __ldg(S.s + S.nv + gi);
-      ndmm = __ldg(S.d + gi);
-      ndgg = __ldg(S.d + S.nv + gi);
-      ndmg = __ldg(S.d + 2 * S.nv + gi);
+      nsmg = __ldg(S.s + gi);
+      nsv = __ldg(S.sv + gi);
     }
   };
   auto solve_out = [&](int z) {
@@ -195,9 +193,11 @@ __global__ void __launch_bounds__(32 * TY, fused_min_blocks(3, TY, R))
       const long long um = (long long)a[5 * ls] * (1LL << K) + a[4 * ls];
       const long long ug = (long long)a[7 * ls] * (1LL << K) + a[6 * ls];
       constexpr long long n = PatchConst<3, R>::N;
+      const size_t gi = ((size_t)z * P.vy + y) * P.vx + x;
       float sigma, m;
-      solve_centred(n * uu - (long long)su * su, ndmm, ndgg, ndmg, n * um - (long long)su * nsm,
-                    n * ug - (long long)su * nsg, P.thr_var, P.thr_m, P.thr_g, P.sig_scale, sigma, m);
+      solve_centred_static(n * uu - (long long)su * su, n * um - (long long)su * nsmg.x,
+                           n * ug - (long long)su * nsmg.y, nsv, S.d, S.nv, gi, P.thr_var,
+                           P.sig_scale, sigma, m);
       acc_m += __float2int_rn(m * P.sum_scale);
       acc_s += __float2int_rn(sigma * P.sum_scale);
     }

@@ -576,6 +576,56 @@ __device__ __forceinline__ void solve_centred(long long d_uu, long long d_mm, lo
   measure = m;
 }
 
+// solve_centred for a static M and G (HighResolutionModality: Fixed): the
+// factors of the static columns come precomputed per voxel in sv --
+// im = rsqrtf(D_mm) when D_mm > thr_m else 0, ig likewise for D_gg, rmg =
+// D_mg im ig (k_fixed_solve_static) -- from the same float operations, so the
+// values are the same bit for bit. The nearly collinear case reads the exact
+// centred sums d[3][nv] of voxel gi.
+__device__ __forceinline__ void solve_centred_static(long long d_uu, long long d_um,
+                                                     long long d_ug, float4 sv,
+                                                     const long long* __restrict__ d, size_t nv,
+                                                     size_t gi, long long thr_var,
+                                                     float sig_scale, float& sigma,
+                                                     float& measure) {
+  sigma = 0.0f;
+  measure = 0.0f;
+  if (d_uu <= thr_var) return;
+  const float fuu = ll2f(d_uu);
+  sigma = sqrtf(fuu) * sig_scale;
+  const float im = sv.x, ig = sv.y;
+  const bool km = im > 0.0f, kg = ig > 0.0f;
+  const float iu = rsqrtf(fuu);
+  float r2 = 0.0f;
+  if (km && kg) {
+    const float rum = ll2f(d_um) * iu * im, rug = ll2f(d_ug) * iu * ig, rmg = sv.z;
+    const float den = 1.0f - rmg * rmg;
+    if (den > 1e-3f) {
+      r2 = __fdividef(rum * rum + rug * rug - 2.0f * rum * rug * rmg, den);
+    } else {
+      // nearly collinear columns: solve in double from the exact sums
+      double duu = (double)d_uu, dmm = (double)__ldg(d + gi), dgg = (double)__ldg(d + nv + gi);
+      double dmg = (double)__ldg(d + 2 * nv + gi), dum = (double)d_um, dug = (double)d_ug;
+      double det = dmm * dgg - dmg * dmg;
+      double e;
+      if (det <= 1e-10 * dmm * dgg)
+        e = dum * dum / dmm;
+      else
+        e = (dgg * dum * dum - 2.0 * dmg * dum * dug + dmm * dug * dug) / det;
+      r2 = (float)(e / duu);
+    }
+  } else if (km) {
+    const float c = ll2f(d_um) * iu * im;
+    r2 = c * c;
+  } else if (kg) {
+    const float c = ll2f(d_ug) * iu * ig;
+    r2 = c * c;
+  }
+  float m = sigma * r2;
+  if (!(m > 0.0f) || isinf(m)) m = 0.0f;
+  measure = m;
+}
+
 // Per-voxel sigma and clipped measure from exact patch sums.
 // Reference semantics: sigma = sqrt(sample variance of U) when every patch
 // value is > 1e-6 and the variance is > 1e-6, else 0; measure =
