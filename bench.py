@@ -876,7 +876,10 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "traffic_source": from_profile,
-                         "kernel": f"{kname} (moments pass; the resample pass is kernels_ms_per_step.warp)",
+                         "kernel": f"{kname} (moments pass"
+                                   + ("; the rows 24-row tiles leave over run on k_fused_ps"
+                                      if kname == "k_fused_pt" else "")
+                                   + "; the resample pass is kernels_ms_per_step.warp)",
                          "launches_per_step": mom_launches,
                          "kernel_ms_per_launch": mom_ms / max(1, mom_launches),
                          "scope": "achieved and traffic are totals of the step's moments launches",

@@ -277,3 +277,19 @@ def test_presample_groups_do_not_change_values(hr_moving):
     np.testing.assert_array_equal(whole, parts)
     np.testing.assert_array_equal([ctx.evaluate(mats[k]) for k in (0, 77, 149)], whole[[0, 77, 149]])
     ctx.close()
+
+
+@pytest.mark.parametrize("us,r", [(20, 2), (45, 4), (40, 2), (52, 3)])
+def test_tall_tiles_on_any_grid_height(us, r):
+    """The 24-row moments kernel on grid heights that it covers alone (20,
+    45: the last tile partly outside) or together with one row of 16-row
+    tiles (40 = 24 + 16, 52 = 48 + 4) gives the bits of the 16-row kernel."""
+    case = synth.case_3d(seed=95 + us, mr_size=us + 8, us_size=us, r=r, blobs=5)
+    ctx = make_context(case, "f16")
+    mats = perturbed(case, np.random.default_rng(us), 7)
+    ctx.set_option(capi.OPTION_TILE_ROWS, 16)
+    ref = ctx.evaluate_batch(mats)
+    ctx.set_option(capi.OPTION_TILE_ROWS, 24)
+    np.testing.assert_array_equal(ctx.evaluate_batch(mats), ref)
+    np.testing.assert_array_equal([ctx.evaluate(m) for m in mats[:2]], ref[:2])
+    ctx.close()
