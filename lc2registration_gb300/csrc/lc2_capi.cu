@@ -634,19 +634,20 @@ int launch_group_generic(lc2_context* c, int k0, int cnt, float* osig, float* om
 }
 
 // Output rows per tile of the fused kernels: the option if set; in 2D 0 (per
-// launch); for the 3D kernels of a resampled MR/CT 24 -- on presampled
-// images at patch radius 1-4 for grids of 8 M voxels or more (k_fused_pt,
+// launch); in 3D 24 -- on presampled images at patch radius 1-4 for grids
+// of 8 M voxels or more, in both modalities (k_fused_pt, k_fused_fixed_pt;
 // 24 warps per SM: at 256^3 2-3 % faster batched and 15 % for one transform
-// than 16-row tiles; on 96^3 grids 4-9 % slower batched, where fewer, taller
-// tiles split z into shorter chunks), resampling in place at radius 3 or 4
-// (one 768-thread CTA per SM) -- else 16.
+// than 16-row tiles with a resampled MR/CT, 2 % with a resampled ultrasound;
+// on 96^3 grids 4-9 % slower batched, where fewer, taller tiles split z into
+// shorter chunks), and for a resampled MR/CT resampled in the kernel at
+// radius 3 or 4 (one 768-thread CTA per SM) -- else 16.
 int tile_rows(const lc2_context* c) {
   if (c->tile_rows > 0) return c->tile_rows;
   if (c->lc2_nd == 2) return 0;  // chosen per launch: 32 rows for large launches, else 16
   const int r = c->cfg.patch_size;
-  if (c->lc2_nd != 3 || !c->cfg.high_res_is_moving) return 16;
+  if (c->lc2_nd != 3) return 16;
   if (c->presample) return (r <= 4 && c->nv >= 8000000) ? 24 : 16;
-  return (r == 3 || r == 4) ? 24 : 16;
+  return (c->cfg.high_res_is_moving && (r == 3 || r == 4)) ? 24 : 16;
 }
 
 // The fused kernel (static ultrasound): one launch for `cnt` transforms.
@@ -866,9 +867,15 @@ int launch_fused_fixed(lc2_context* c, int k0, int cnt) {
     // the ultrasound resampled in a pass of its own, then the moments, in
     // groups of the presample buffer's capacity
     LC2_TRY(ensure_presample(c, cnt));
-    // k_fused_fixed3's tile height and CTAs per SM
-    const int ty = (c->cfg.patch_size > 4 || L.tile_height == 8) ? 8 : 16;
-    const int group = presample_group(c, cnt, ty, lc2::fused_min_blocks(3, ty, c->cfg.patch_size));
+    // the moments kernel's tile height and CTAs per SM: 24 rows
+    // (k_fused_fixed_pt, the rows it leaves over on 16-row tiles), else
+    // k_fused_fixed3's 16 or 8
+    const int ty = c->cfg.patch_size > 4 || L.tile_height == 8 ? 8
+                   : L.tile_height == 24                       ? 24
+                                                               : 16;
+    const int group =
+        presample_group(c, cnt, ty, ty == 24 ? 1 : lc2::fused_min_blocks(3, ty, c->cfg.patch_size));
+    const int rest = ty == 24 ? pt_rest_rows(c) : 0;
     for (int j = 0; j < cnt; j += group) {
       const int n = std::min(group, cnt - j);
       {
@@ -886,8 +893,19 @@ int launch_fused_fixed(lc2_context* c, int k0, int cnt) {
       L.k0 = k0 + j;
       L.cnt = n;
       L.pre = c->d_pre;
+      L.y_off = 0;
+      L.y_rows = c->virt.dim[1] - rest;
       e = fixed();
       ++c->launches;
+      if (e == cudaSuccess && rest) {
+        L.tile_height = 16;
+        L.y_off = c->virt.dim[1] - rest;
+        L.y_rows = rest;
+        e = fixed();
+        ++c->launches;
+        L.tile_height = 24;
+      }
+      L.y_off = L.y_rows = 0;
       if (e != cudaSuccess)
         return fail(LC2_ERR_CUDA, "fused kernel (resampled ultrasound): %s", cudaGetErrorString(e));
     }
@@ -2625,10 +2643,10 @@ extern "C" int lc2_autotune(lc2_context* c, const float* matrices, int count, in
   const bool hrm = c->cfg.high_res_is_moving != 0;
   if (c->lc2_nd == 3 && !c->mi && !c->generic) {
     LC2_TRY(lc2_stage_transforms(c, matrices, count));
-    // 24-row tiles exist for the kernel of a resampled MR/CT only
+    // 24-row tiles exist for the presampled 3D kernels
     std::vector<int> rows = (r > 4) ? std::vector<int>{8}
-                            : hrm   ? std::vector<int>{16, 24, 8}
-                                    : std::vector<int>{16, 8};
+                            : (hrm || c->presample) ? std::vector<int>{16, 24, 8}
+                                                    : std::vector<int>{16, 8};
     const int vz = c->virt.dim[2];
     std::vector<int> chunks{0};
     for (int zc : {vz, vz / 2, vz / 4, 64, 32})

@@ -203,7 +203,8 @@ def test_presample_forms(r, storage):
 @pytest.mark.parametrize("r,storage", [(2, "f32"), (4, "f16")])
 def test_presample_fixed_modality(r, storage):
     """HighResolutionModality: Fixed with the warped ultrasound presampled (the
-    default for 3D): the same bits whatever the tile height, z chunk or batch,
+    default for 3D): the same bits whatever the tile height (the 768-thread
+    kernel at 24 rows), z chunk or batch,
     within FP32 resampling rounding of the in-kernel resampling, and within
     1e-5 of the FP64 oracle."""
     from tests.helpers import oracle_eval
@@ -217,7 +218,7 @@ def test_presample_fixed_modality(r, storage):
     mats = mats.astype(np.float32)
     ref = ctx.evaluate_batch(mats)
     np.testing.assert_array_equal([ctx.evaluate(m) for m in mats[:2]], ref[:2])
-    for rows in (16, 8):
+    for rows in (16, 24, 8):
         ctx.set_option(capi.OPTION_TILE_ROWS, rows)
         for zc in (0, 7):
             ctx.set_option(capi.OPTION_ZCHUNK, zc)
@@ -287,6 +288,26 @@ def test_tall_tiles_on_any_grid_height(us, r):
     case = synth.case_3d(seed=95 + us, mr_size=us + 8, us_size=us, r=r, blobs=5)
     ctx = make_context(case, "f16")
     mats = perturbed(case, np.random.default_rng(us), 7)
+    ctx.set_option(capi.OPTION_TILE_ROWS, 16)
+    ref = ctx.evaluate_batch(mats)
+    ctx.set_option(capi.OPTION_TILE_ROWS, 24)
+    np.testing.assert_array_equal(ctx.evaluate_batch(mats), ref)
+    np.testing.assert_array_equal([ctx.evaluate(m) for m in mats[:2]], ref[:2])
+    ctx.close()
+
+
+@pytest.mark.parametrize("us,r", [(20, 2), (45, 4), (40, 3)])
+def test_tall_tiles_fixed_modality(us, r):
+    """The 24-row kernel of HighResolutionModality: Fixed, alone (20, 45 rows)
+    or with a row of 16-row tiles (40 = 24 + 16), gives the bits of the 16-row
+    kernel."""
+    base = synth.case_3d(seed=97 + us, mr_size=us + 8, us_size=us, r=r, blobs=5)
+    inv = np.linalg.inv(base.true_mat.astype(np.float64)).astype(np.float32)
+    case = synth.Case(base.mode, base.moving_geom, base.moving, base.fixed_geom, base.fixed,
+                      [1.0, 1.0, 1.0], r, hr_moving=False, true_params={}, true_mat=inv)
+    ctx = make_context(case, "f16")
+    mats = np.linalg.inv(perturbed(base, np.random.default_rng(us), 7).astype(np.float64))
+    mats = mats.astype(np.float32)
     ctx.set_option(capi.OPTION_TILE_ROWS, 16)
     ref = ctx.evaluate_batch(mats)
     ctx.set_option(capi.OPTION_TILE_ROWS, 24)
