@@ -3,7 +3,7 @@
 image, the ultrasound is warped per transform) against the FP64 oracle and
 against the generic path (LC2_OPTION_GENERIC), through the C ABI.
 
-Tolerances: LC2 within 1e-5 relative of the oracle (the north-star bound);
+Tolerances: LC2 within 1e-5 relative of the oracle;
 fused against generic within 1e-6 relative (the two place their sampling
 bases differently, so an interpolated value can differ in its last bit and a
 quantised ultrasound value by one step); tile heights, batch vs plain: bit-

@@ -1,7 +1,7 @@
 """GPU parity of the CUDA LC2 path against the FP64 oracle (through the C ABI).
 
 Tolerances:
-  * LC2 value: 1e-5 relative to the oracle (the benchmark spec's bound);
+  * LC2 value: 1e-5 relative to the oracle;
   * warped image M and its Sobel magnitude G: 2e-5 of the image's range
     (FP32 resampling vs FP64; coordinates agree to ~1e-6 voxel);
   * sigma: 1e-5 relative where both are non-zero, identical zero pattern
