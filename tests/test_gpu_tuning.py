@@ -314,3 +314,19 @@ def test_tall_tiles_fixed_modality(us, r):
     np.testing.assert_array_equal(ctx.evaluate_batch(mats), ref)
     np.testing.assert_array_equal([ctx.evaluate(m) for m in mats[:2]], ref[:2])
     ctx.close()
+
+
+def test_weighting_map_on_tall_tiles():
+    """The per-voxel measure written by the moments pass (lc2_weighting_map)
+    is the same with 24-row tiles plus a row of 16-row tiles (a 40-row grid)
+    as with 16-row tiles alone."""
+    case = synth.case_3d(seed=99, mr_size=48, us_size=40, r=3, blobs=5)
+    ctx = make_context(case, "f16")
+    ctx.set_option(capi.OPTION_TILE_ROWS, 16)
+    v16, m16 = ctx.weighting_map(case.true_mat)
+    ctx.set_option(capi.OPTION_TILE_ROWS, 24)
+    v24, m24 = ctx.weighting_map(case.true_mat)
+    assert v24 == v16
+    np.testing.assert_array_equal(m24, m16)
+    assert np.count_nonzero(m16) > 0
+    ctx.close()
