@@ -154,19 +154,19 @@ int lc2_warp_affine_2d(const float* src, int sw, int sh, float* dst, int dw, int
 long long lc2_launch_count(const lc2_context* ctx);
 
 /* Tuning options (lc2_set_option). LC2_OPTION_TILE_ROWS: output rows per
- * tile of the fused 3D kernel: 16 (one CTA per SM), 24 (one 768-thread CTA
- * per SM; resampled MR/CT only, the resampled-ultrasound kernel takes it as
- * 16) or 8 (two per SM); 0 = automatic (for a resampled MR/CT 24 at patch
- * radius 1-4 on presampled images of grids of 8 M voxels or more and at
- * radius 3 or 4 when the kernel resamples itself, LC2_OPTION_PRESAMPLE 0;
- * else 16). On presampled images
- * at radius 1-4, 24 selects the 768-thread moments kernel and 8 or 16 the
- * 512-thread one. 2D and 2D-to-3D contexts with a resampled MR/CT: 16 or
- * 32 (two 1024-thread CTAs per SM, patch radius 4 to 6; other radii take
- * it as 16); 0 = per launch (32 where it exists and the launch has four
- * CTAs per SM or more). No counterpart in the
- * reference (its block sizes are arguments of CalculateGradient /
- * GetSimilarityMetric, src/cu_LC2/cu_lc2_3d.cuh:36-41). */
+ * tile of the fused 3D kernels at patch radius 1-4: 16 (one 512-thread CTA
+ * per SM), 24 (one 768-thread CTA per SM; on presampled images, and for a
+ * resampled MR/CT resampled in the kernel; elsewhere taken as 16; a grid
+ * whose height leaves 1-16 rows over runs them on 16-row tiles) or 8 (two
+ * CTAs per SM); radius 5-6 always runs 8. 0 = automatic: 24 on presampled
+ * images -- of a resampled MR/CT on any grid, of a resampled ultrasound on
+ * grids of 8 M voxels or more -- and for a resampled MR/CT at radius 3 or 4
+ * when the kernel resamples itself (LC2_OPTION_PRESAMPLE 0); else 16. 2D and
+ * 2D-to-3D contexts with a resampled MR/CT: 16 or 32 (two 1024-thread CTAs
+ * per SM, patch radius 4 to 6; other radii take it as 16); 0 = per launch
+ * (32 where it exists and the launch has four CTAs per SM or more). No
+ * counterpart in the reference (its block sizes are arguments of
+ * CalculateGradient / GetSimilarityMetric, src/cu_LC2/cu_lc2_3d.cuh:36-41). */
 enum { LC2_OPTION_TILE_ROWS = 1 };
 /* LC2_OPTION_ZCHUNK: output slices each CTA of the fused 3D kernel marches
  * through (0 = automatic). LC2_OPTION_GRAPHS: 1 (default) replays

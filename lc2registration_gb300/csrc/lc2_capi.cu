@@ -634,20 +634,20 @@ int launch_group_generic(lc2_context* c, int k0, int cnt, float* osig, float* om
 }
 
 // Output rows per tile of the fused kernels: the option if set; in 2D 0 (per
-// launch); in 3D 24 -- on presampled images at patch radius 1-4 for grids
-// of 8 M voxels or more, in both modalities (k_fused_pt, k_fused_fixed_pt;
-// 24 warps per SM: at 256^3 2-3 % faster batched and 15 % for one transform
-// than 16-row tiles with a resampled MR/CT, 2 % with a resampled ultrasound;
-// on 96^3 grids 4-9 % slower batched, where fewer, taller tiles split z into
-// shorter chunks), and for a resampled MR/CT resampled in the kernel at
-// radius 3 or 4 (one 768-thread CTA per SM) -- else 16.
+// launch); in 3D at patch radius 1-4, 24 -- on presampled images of a
+// resampled MR/CT (k_fused_pt: batched 4-14 % faster than 16-row tiles from
+// 48^3 to 256^3 grids, one transform per call up to 15 %), on a presampled
+// ultrasound for grids of 8 M voxels or more (k_fused_fixed_pt: at 256^3
+// 1.4 % batched and 5 % per call; on 48^3 to 160^3 grids 16 rows were up to
+// 3 % faster), and for a resampled MR/CT resampled in the kernel at radius 3
+// or 4 (one 768-thread CTA per SM) -- else 16.
 int tile_rows(const lc2_context* c) {
   if (c->tile_rows > 0) return c->tile_rows;
   if (c->lc2_nd == 2) return 0;  // chosen per launch: 32 rows for large launches, else 16
   const int r = c->cfg.patch_size;
-  if (c->lc2_nd != 3) return 16;
-  if (c->presample) return (r <= 4 && c->nv >= 8000000) ? 24 : 16;
-  return (c->cfg.high_res_is_moving && (r == 3 || r == 4)) ? 24 : 16;
+  if (c->lc2_nd != 3 || r > 4) return 16;
+  if (c->presample) return (c->cfg.high_res_is_moving || c->nv >= 8000000) ? 24 : 16;
+  return (c->cfg.high_res_is_moving && r >= 3) ? 24 : 16;
 }
 
 // The fused kernel (static ultrasound): one launch for `cnt` transforms.

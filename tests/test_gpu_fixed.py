@@ -90,11 +90,14 @@ def test_fixed_reduced_storage_matches_oracle_on_rounded_inputs(kind, storage):
 
 
 def test_fixed_autotune_keeps_values():
+    """The autotuner picks a tile height among 8, 16 and 24 rows (the
+    768-thread kernel on the presampled ultrasound) and the values stay the
+    same bits."""
     case, mats = _fixed("3d_r3", 4)
     ctx = make_context(case)
     before = ctx.evaluate_batch(mats)
     rows, zc = ctx.autotune(mats)
-    assert rows in (8, 16)
+    assert rows in (8, 16, 24)
     assert np.array_equal(ctx.evaluate_batch(mats), before)
 
 
