@@ -11,7 +11,9 @@ transforms.
     512 candidate affines in one launch, f16 and bf16 storage (the
     benchmark's main line), with HighResolutionModality Moving and Fixed;
   * 2D 256^2, 7x7 patches, 512 affines per launch, f32;
-  * 3D 128^3 -> 96^3, 7^3 patches, 256 affines per launch, f32.
+  * 3D 128^3 -> 96^3, 7^3 patches, 256 affines per launch, f32;
+  * 3D 200^3, 7^3 patches, 64 affines per launch, f32 (24-row tiles and one
+    row of 16-row tiles for the 8 rows they leave over).
 
 The oracle is fed the same storage-rounded volumes. Tolerance: 1e-5
 relative on LC2.
@@ -77,3 +79,12 @@ def test_3d_128_to_96_batch_matches_oracle():
     case = synth.case_3d(seed=8, mr_size=128, us_size=96, r=3)
     mats = perturbed(case, np.random.default_rng(3), 256)
     _check(case, mats, "f32", [0, 1, 100, 200, 255])
+
+
+def test_200cubed_split_tiles_match_oracle():
+    """A 200-row grid: 24-row tiles over rows 0-191 and one row of 16-row
+    tiles over rows 192-199 (8 of its 16 rows outside the grid), radius 3,
+    FP32, 64 transforms per launch."""
+    case = synth.case_3d(seed=9, mr_size=200, us_size=200, r=3)
+    mats = perturbed(case, np.random.default_rng(4), 64)
+    _check(case, mats, "f32", [0, 31, 63])
